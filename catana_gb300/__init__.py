@@ -1,0 +1,17 @@
+"""catana_gb300 -- GB300-native (sm_103a) spherical Fourier-Bessel decomposition.
+
+Drop-in for the decomposition path of CatAna's Python package (python/catana/
+__init__.py): ``PointContainer``, ``PixelizedPointContainer``, ``Point``,
+``sfb_decomposition`` (raw and HEALPix overloads), ``KClkk`` and
+``besseltools.SphericalBesselZeros`` keep the reference's names, arguments and
+errors.  The compute runs in libcatana_gpu.so (hand-written CUDA for sm_103a behind
+the C ABI in include/catana_gpu.h); there is no CPU fallback.
+"""
+from . import _lib  # noqa: F401  (raises ImportError when the library is missing)
+from . import besseltools
+from .basictypes import PixelizedPointContainer, Point, PointContainer
+from .decomposition import KClkk, compute_kln, sfb_decomposition, sfb_decomposition_healpix
+
+__all__ = ["Point", "PointContainer", "PixelizedPointContainer", "KClkk", "sfb_decomposition",
+           "sfb_decomposition_healpix", "compute_kln", "besseltools"]
+__version__ = "0.1.0"

@@ -1,0 +1,79 @@
+"""ctypes binding of libcatana_gpu.so (the C ABI in include/catana_gpu.h).
+
+The library is built in-tree by ``catana_gb300.build`` into ``catana_gb300/_lib/``.
+Loading it needs no GPU; calling its compute entry points does.  There is no CPU
+fallback: if the library is missing, importing this module raises ImportError.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcatana_gpu.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        "libcatana_gpu.so not found at %s; build it with `python -m catana_gb300.build` "
+        "(nvcc for sm_103a). catana_gb300 has no CPU fallback." % LIB_PATH)
+
+lib = ctypes.CDLL(LIB_PATH)
+
+_D = ctypes.c_double
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_U16 = ctypes.c_uint16
+_U32 = ctypes.c_uint32
+_I32 = ctypes.c_int32
+
+# status codes (catana_status_t)
+OK, ERR_ARG, ERR_DOMAIN, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED = range(6)
+# flags
+JL_AUTO, JL_INTERP, JL_EXACT = 0, 1, 2
+FORM_PLAIN, FORM_SPLIT = 0, 4
+HEALPIX_CONJ_FIX = 8
+
+SIGNATURES = {
+    "catana_gpu_flmn_size": (ctypes.c_size_t, [_U16, _U16]),
+    "catana_gpu_sfb_raw": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
+    "catana_gpu_sfb_raw_dev": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P, _P]),
+    "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
+    "catana_gpu_bin_points": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
+    "catana_gpu_ang2pix_ring": (ctypes.c_int, [_I64, _P, _P, _I64, _P, _P]),
+    "catana_gpu_pix2ang_ring": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
+    "catana_gpu_sbessel_zeros": (ctypes.c_int, [_U32, _I32, _P]),
+    "catana_gpu_compute_kln": (ctypes.c_int, [_U16, _U16, _D, _P]),
+    "catana_gpu_last_error": (ctypes.c_char_p, []),
+    "catana_gpu_launch_count": (ctypes.c_uint64, []),
+}
+
+for _name, (_res, _args) in SIGNATURES.items():
+    if hasattr(lib, _name):
+        _f = getattr(lib, _name)
+        _f.restype = _res
+        _f.argtypes = _args
+
+
+def last_error():
+    return lib.catana_gpu_last_error().decode(errors="replace")
+
+
+class CatanaError(RuntimeError):
+    pass
+
+
+def check(status, what=""):
+    """Map a catana_status_t to the exception the reference's bindings raise."""
+    if status == OK:
+        return
+    msg = last_error() or what
+    if status in (ERR_ARG, ERR_DOMAIN):
+        raise ValueError(msg)
+    if status == ERR_NOMEM:
+        raise MemoryError(msg)
+    raise CatanaError("catana_gpu error %d: %s" % (status, msg))
+
+
+def ptr(a):
+    """Data pointer of a numpy array (None for None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.c_void_p)

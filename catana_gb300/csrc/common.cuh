@@ -1,0 +1,116 @@
+// common.cuh -- shared declarations of the catana_gpu library (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/catana_gpu.h"
+
+namespace catana_gpu {
+
+// Launch counter behind catana_gpu_launch_count().
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void set_error(const std::string &msg);
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t cap = need + need / 4;
+        cudaError_t e = cudaMalloc(&ptr, cap);
+        if (e == cudaSuccess) bytes = cap;
+        return e;
+    }
+    template <class T> T *as() const { return reinterpret_cast<T *>(ptr); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+// Per-device state: workspace and cached tables.  Guarded by `mu`.
+struct DeviceContext {
+    std::mutex mu;
+    int device = 0;
+    int sm_count = 0;
+    int cc_major = 0, cc_minor = 0;
+    // workspace
+    DevBuf soa;        // point SoA (r, x, phi, w) of the current chunk
+    DevBuf state;      // Legendre recurrence rows
+    DevBuf partial;    // per-slab partial sums
+    DevBuf flmn;       // f_lmn accumulator (complex, packed)
+    DevBuf kln;        // k_ln on device
+    DevBuf coef;       // Legendre recurrence coefficients
+    DevBuf tables;     // j_l interpolation tables (FP64 lerp)
+    DevBuf misc;       // error word, small scalars
+    DevBuf io_points;  // staging of host inputs
+    DevBuf io_out;     // staging of outputs
+    DevBuf split_ws;   // split-form workspace
+    DevBuf hp_ws;      // HEALPix workspace
+    // cache keys
+    int coef_lmax = -1;
+    int tab_lmax = -1, tab_nmax = -1;
+    std::vector<double> tab_dxinv, tab_zmax;  // per l
+};
+
+DeviceContext *get_context(int *status);
+
+// Bessel zeros (host, cached): z[l][n] for n < count.  Thread-safe.
+const double *zeros_for(unsigned l, int count);
+// k_ln table row-major (lmax x nmax), host.
+void kln_table(int lmax, int nmax, double rmax, double *out);
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+#define CG_CUDA_TRY(expr)                                                                        \
+    do {                                                                                         \
+        cudaError_t _e = (expr);                                                                 \
+        if (_e != cudaSuccess) {                                                                 \
+            ::catana_gpu::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+            return _e == cudaErrorMemoryAllocation ? CATANA_ERR_NOMEM : CATANA_ERR_CUDA;          \
+        }                                                                                        \
+    } while (0)
+
+// FP64 plain raw path (sfb_fp64.cu).  All pointers device.  Accumulates into
+// f_acc (complex, packed by l, un-normalised); the caller normalises.
+catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
+                                    int64_t npoints, int lmax, int nmax, bool interpolated, const double *kln_dev,
+                                    double *f_acc_dev, int *err_dev, cudaStream_t st);
+// f *= norm; c_ln from f (device).
+catana_status_t finish_flmn_cln(double *f_dev, double norm, int lmax, int nmax, double *c_ln_dev,
+                                cudaStream_t st);
+// FP64 lerp tables (1000*nmax nodes per l) for l < lmax, cached in ctx->tables.
+catana_status_t ensure_lerp_tables(DeviceContext *ctx, int lmax, int nmax, cudaStream_t st);
+// Legendre coefficients for l < lmax, cached in ctx->coef.
+catana_status_t ensure_coefs(DeviceContext *ctx, int lmax, cudaStream_t st);
+
+// Split (tensor-core) raw path (sfb_split.cu).
+catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
+                                     int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
+                                     double *f_acc_dev, int *err_dev, cudaStream_t st);
+
+// HEALPix (healpix.cu).
+catana_status_t healpix_bin_dev(DeviceContext *ctx, int64_t nside, const double *points_dev, int64_t npoints,
+                                int64_t *offsets_dev, double *r_sorted_dev, int *err_dev, cudaStream_t st);
+catana_status_t healpix_ang2pix_dev(int64_t nside, const double *theta, const double *phi, int64_t n,
+                                    int64_t *pix, int *err_dev, cudaStream_t st);
+catana_status_t healpix_pix2ang_dev(int64_t nside, const int64_t *pix, int64_t n, double *theta, double *phi,
+                                    cudaStream_t st);
+catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t *offsets_dev,
+                                const double *r_sorted_dev, int64_t npoints, int lmax, int nmax, bool interpolated,
+                                bool conj_fix, const double *kln_dev, double norm, double *f_dev, double *c_ln_dev,
+                                int *err_dev, cudaStream_t st);
+
+}  // namespace catana_gpu

@@ -1,0 +1,409 @@
+// sfb_fp64.cu -- the plain FP64 raw SFB path on CUDA cores (the drop-in form).
+//
+// Reference: _sfb_raw, sfb_raw.cpp:13-108.  The reference loops l outermost and,
+// per point, evaluates j_l(k_ln r) for every n (:67-69), P_lm by gsl_sf_legendre_sphPlm
+// for every m <= l (:72-74, O(l-m) each) and accumulates k j Y* (:76-78); thread
+// partial sums are combined under `omp critical` (:81-84).
+//
+// GPU form, per multipole l and per chunk of points:
+//   * the Legendre values advance by one step of the l-recurrence from two stored
+//     rows P_{l-1}^m, P_{l-2}^m (FP64 [m][point] arrays in HBM), so each P_lm costs
+//     O(1) instead of O(l-m);
+//   * e^{-im phi} comes from one sincos per thread and m-run plus complex rotation;
+//   * j_l comes from the reference's own linear table (1000*nmax nodes up to
+//     z_{l,nmax}, same node placement, same dx_inv, same lerp) or, in exact mode,
+//     from the direct evaluation in special.cuh;
+//   * a CTA owns a slab of points and a TILE x TILE block of (m, n); it stages
+//     J[n][pt] and Y[m][pt] for 32 points in shared memory and accumulates f(m,n) in
+//     FP64 registers (TILE/16 x TILE/16 complex per thread);
+//   * slabs write partial tiles; a second kernel sums them in slab order into the
+//     f_lmn accumulator (deterministic, no atomics).
+// The FP64 pipe bounds this path: 2*nmax*(l+1) FMAs per point per l.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "special.cuh"
+
+namespace catana_gpu {
+
+namespace {
+
+constexpr int kTP = 32;        // points per shared-memory step
+constexpr int kThreads = 256;  // threads per CTA
+
+// AoS (r, theta, phi) -> SoA r, x = cos(theta), phi, w.
+__global__ void k_prep_points(const double *__restrict__ pts, const double *__restrict__ w, int64_t n,
+                              double *__restrict__ r_o, double *__restrict__ x_o, double *__restrict__ ph_o,
+                              double *__restrict__ w_o) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    r_o[i] = pts[3 * i];
+    x_o[i] = cos(pts[3 * i + 1]);
+    ph_o[i] = pts[3 * i + 2];
+    w_o[i] = w ? w[i] : 1.0;
+}
+
+// y[l][i] = j_l(0 + i*dx_l): FunctionInterpolator.cpp:12-19 with the node formula
+// x_min + i*dx of the reference.
+__global__ void k_lerp_tables(double *__restrict__ tab, const double *__restrict__ dx, int lmax, int npts) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)lmax * npts) return;
+    int l = (int)(t / npts);
+    int i = (int)(t - (int64_t)l * npts);
+    tab[t] = sbessel_jl(l, 0.0 + (double)(size_t)i * dx[l]);
+}
+
+struct LArgs {
+    int l, nmax, nslabs;
+    int64_t n;  // points in the chunk
+    const double *r, *x, *ph, *w;
+    const double *kln;  // k_ln row of l (nmax)
+    const double *tab;  // lerp table of l, or null for exact j_l
+    int npts_tab;
+    double dx_inv, zmax;
+    const double *st1, *st2;  // P_{l-1}^m, P_{l-2}^m rows: [m][n]
+    double *st0;              // P_l^m out
+    const double2 *coef;      // recurrence coefficients of l (m = 0..l)
+    double2 *partial;         // [slab][m][nmax]
+    int *err;
+};
+
+template <int TILE>
+__global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
+    constexpr int TT = TILE / 16;     // per-thread accumulator tile
+    constexpr int LD = TILE + 1;      // padded row of the staged tiles
+    constexpr int PER_G = TILE / 8;   // items per generator thread
+    extern __shared__ double smem[];
+    double *sJ = smem;                // [kTP][LD]
+    double *sYr = sJ + kTP * LD;      // [kTP][LD]
+    double *sYi = sYr + kTP * LD;     // [kTP][LD]
+
+    const int l = a.l;
+    const int slab = blockIdx.x;
+    const int m0 = blockIdx.y * TILE, n0 = blockIdx.z * TILE;
+    const int mcount = min(TILE, l + 1 - m0), ncount = min(TILE, a.nmax - n0);
+    const int64_t per = ((a.n + a.nslabs - 1) / a.nslabs + kTP - 1) / kTP * kTP;
+    const int64_t i0 = (int64_t)slab * per, i1 = min(a.n, i0 + per);
+
+    const int tid = threadIdx.x;
+    const int q = tid % kTP, g = tid / kTP;   // generator: point q, group g
+    const int tx = tid % 16, ty = tid / 16;   // contraction: n = tx+16b, m = ty+16a
+    const bool write_state = (blockIdx.z == 0);
+
+    double accR[TT][TT], accI[TT][TT];
+#pragma unroll
+    for (int u = 0; u < TT; ++u)
+#pragma unroll
+        for (int v = 0; v < TT; ++v) accR[u][v] = accI[u][v] = 0.0;
+
+    const double inv_sqrt4pi = 0.28209479177387814347403972578038630;  // 1/sqrt(4 pi)
+
+    for (int64_t base = i0; base < i1; base += kTP) {
+        const int64_t i = base + q;
+        const bool valid = i < i1;
+        double r = 0.0, x = 0.0, ph = 0.0, wi = 0.0;
+        if (valid) {
+            r = a.r[i];
+            x = a.x[i];
+            ph = a.ph[i];
+            wi = a.w[i];
+        }
+        // ---- J[pt][n] = k_ln j_l(k_ln r) w ----
+#pragma unroll
+        for (int k = 0; k < PER_G; ++k) {
+            const int nl = g + 8 * k;
+            double val = 0.0;
+            if (valid && nl < ncount) {
+                const double kk = a.kln[n0 + nl];
+                const double z = kk * r;
+                double j;
+                if (a.tab) {
+                    if (!(z >= 0.0) || z >= a.zmax) {  // beyond the table (or a negative / NaN radius)
+                        *a.err = CATANA_ERR_DOMAIN;
+                        j = 0.0;
+                    } else {
+                        const double ia = z * a.dx_inv;
+                        int ii = (int)ia;
+                        if (ii > a.npts_tab - 2) ii = a.npts_tab - 2;
+                        const double y0 = a.tab[ii], y1 = a.tab[ii + 1];
+                        j = y0 + (y1 - y0) * (ia - ii);
+                    }
+                } else {
+                    j = sbessel_jl(l, z);
+                }
+                val = kk * j * wi;
+            }
+            sJ[q * LD + nl] = val;
+        }
+        // ---- Y[pt][m] = P_lm(x) e^{-i m phi}, P by one recurrence step ----
+        {
+            const int ml0 = g * PER_G;
+            double sn, cs;
+            sincos((double)(m0 + ml0) * ph, &sn, &cs);
+            double er = cs, ei = -sn;  // e^{-i m phi}
+            double s1, c1;
+            sincos(ph, &s1, &c1);
+#pragma unroll
+            for (int k = 0; k < PER_G; ++k) {
+                const int ml = ml0 + k;
+                const int m = m0 + ml;
+                double P = 0.0;
+                if (valid && ml < mcount) {
+                    if (l == 0) {
+                        P = inv_sqrt4pi;
+                    } else {
+                        const double2 c = a.coef[m];
+                        if (m == l) {
+                            const double somx2 = sqrt((1.0 - x) * (1.0 + x));
+                            P = c.x * somx2 * a.st1[(int64_t)(l - 1) * a.n + i];
+                        } else if (m == l - 1) {
+                            P = c.x * (x * a.st1[(int64_t)m * a.n + i]);
+                        } else {
+                            P = c.x * (x * a.st1[(int64_t)m * a.n + i] - c.y * a.st2[(int64_t)m * a.n + i]);
+                        }
+                    }
+                    if (write_state) a.st0[(int64_t)m * a.n + i] = P;
+                }
+                sYr[q * LD + ml] = P * er;
+                sYi[q * LD + ml] = P * ei;
+                const double nr = er * c1 + ei * s1;
+                const double ni = ei * c1 - er * s1;
+                er = nr;
+                ei = ni;
+            }
+        }
+        __syncthreads();
+        // ---- f(m, n) += J(n) Y(m) ----
+#pragma unroll 4
+        for (int pp = 0; pp < kTP; ++pp) {
+            double jv[TT], yr[TT], yi[TT];
+#pragma unroll
+            for (int u = 0; u < TT; ++u) {
+                yr[u] = sYr[pp * LD + ty + 16 * u];
+                yi[u] = sYi[pp * LD + ty + 16 * u];
+                jv[u] = sJ[pp * LD + tx + 16 * u];
+            }
+#pragma unroll
+            for (int u = 0; u < TT; ++u)
+#pragma unroll
+                for (int v = 0; v < TT; ++v) {
+                    accR[u][v] = fma(jv[v], yr[u], accR[u][v]);
+                    accI[u][v] = fma(jv[v], yi[u], accI[u][v]);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < TT; ++u)
+#pragma unroll
+        for (int v = 0; v < TT; ++v) {
+            const int m = m0 + ty + 16 * u, n = n0 + tx + 16 * v;
+            if (m < l + 1 && n < a.nmax)
+                a.partial[((int64_t)slab * (l + 1) + m) * a.nmax + n] = make_double2(accR[u][v], accI[u][v]);
+        }
+}
+
+// f_acc[l block][m][n] += sum over slabs, in slab order.
+__global__ void k_sum_partials(const double2 *__restrict__ partial, int nslabs, int count, double2 *__restrict__ f) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    double sr = 0.0, si = 0.0;
+    for (int s = 0; s < nslabs; ++s) {
+        const double2 v = partial[(int64_t)s * count + t];
+        sr += v.x;
+        si += v.y;
+    }
+    double2 o = f[t];
+    o.x += sr;
+    o.y += si;
+    f[t] = o;
+}
+
+// f *= norm, then C_ln = sum_{m=-l..l} |f_{l|m|n}|^2 / (2l+1) (sfb_raw.cpp:89-96).
+__global__ void k_finish(double2 *__restrict__ f, double norm, int lmax, int nmax, double *__restrict__ c_ln) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lmax * nmax) return;
+    const int l = t / nmax, n = t - l * nmax;
+    double2 *fl = f + (int64_t)nmax * l * (l + 1) / 2;
+    for (int m = 0; m <= l; ++m) {
+        double2 v = fl[m * nmax + n];
+        v.x *= norm;
+        v.y *= norm;
+        fl[m * nmax + n] = v;
+    }
+    double c = 0.0;
+    for (int m = -l; m <= l; ++m) {
+        const double2 v = fl[(m < 0 ? -m : m) * nmax + n];
+        c += v.x * v.x + v.y * v.y;
+    }
+    c_ln[t] = c / (2 * l + 1);
+}
+
+}  // namespace
+
+catana_status_t ensure_coefs(DeviceContext *ctx, int lmax, cudaStream_t st) {
+    if (ctx->coef_lmax >= lmax) return CATANA_OK;
+    const int L = std::max(lmax, 2);
+    std::vector<double> h((size_t)L * (L + 1));  // (a, b) pairs, triangular by l
+    for (int l = 0; l < L; ++l) {
+        double *row = h.data() + (size_t)l * (l + 1);
+        for (int m = 0; m <= l; ++m) {
+            double ca = 0.0, cb = 0.0;
+            if (l >= 1 && m == l) {
+                ca = -sqrt((2.0 * l + 1.0) / (2.0 * l));
+            } else if (l >= 1 && m == l - 1) {
+                ca = sqrt(2.0 * l + 1.0);
+            } else if (l >= 2) {
+                const double dl = l, dl1 = l - 1, mm = (double)m * m;
+                ca = sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+                cb = sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
+            }
+            row[2 * m] = ca;
+            row[2 * m + 1] = cb;
+        }
+    }
+    CG_CUDA_TRY(ctx->coef.ensure(h.size() * sizeof(double)));
+    CG_CUDA_TRY(cudaMemcpyAsync(ctx->coef.ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    ctx->coef_lmax = L;
+    return CATANA_OK;
+}
+
+catana_status_t ensure_lerp_tables(DeviceContext *ctx, int lmax, int nmax, cudaStream_t st) {
+    if (ctx->tab_lmax >= lmax && ctx->tab_nmax == nmax) return CATANA_OK;
+    const int npts = 1000 * nmax;  // BESSELINTERPOLATIONPOINTS_PER_ZERO * nmax
+    std::vector<double> dx(lmax);
+    ctx->tab_dxinv.assign(lmax, 0.0);
+    ctx->tab_zmax.assign(lmax, 0.0);
+    for (int l = 0; l < lmax; ++l) {
+        const double zmax = zeros_for((unsigned)l, nmax + 1)[nmax];  // SBZ(l)[nmax]
+        dx[l] = (zmax - 0.0) / (npts - 1);
+        ctx->tab_dxinv[l] = 1. / dx[l];
+        ctx->tab_zmax[l] = zmax;
+    }
+    CG_CUDA_TRY(ctx->tables.ensure((size_t)lmax * npts * sizeof(double) + 256 + lmax * sizeof(double)));
+    double *tab = ctx->tables.as<double>();
+    double *dxd = tab + (size_t)lmax * npts;
+    CG_CUDA_TRY(cudaMemcpyAsync(dxd, dx.data(), lmax * sizeof(double), cudaMemcpyHostToDevice, st));
+    const int64_t total = (int64_t)lmax * npts;
+    k_lerp_tables<<<ceil_div(total, 256), 256, 0, st>>>(tab, dxd, lmax, npts);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    ctx->tab_lmax = lmax;
+    ctx->tab_nmax = nmax;
+    return CATANA_OK;
+}
+
+catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
+                                    int64_t npoints, int lmax, int nmax, bool interpolated, const double *kln_dev,
+                                    double *f_acc_dev, int *err_dev, cudaStream_t st) {
+    catana_status_t s = ensure_coefs(ctx, lmax, st);
+    if (s != CATANA_OK) return s;
+    if (interpolated) {
+        s = ensure_lerp_tables(ctx, lmax, nmax, st);
+        if (s != CATANA_OK) return s;
+    }
+    if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
+    // Chunk so that the three Legendre rows stay under ~1.5 GB.
+    int64_t chunk = (int64_t)(1.5e9 / (3.0 * 8.0 * std::max(lmax, 1)));
+    chunk = std::max<int64_t>(1024, std::min<int64_t>(chunk, npoints));
+    CG_CUDA_TRY(ctx->soa.ensure((size_t)chunk * 4 * sizeof(double)));
+    CG_CUDA_TRY(ctx->state.ensure((size_t)chunk * 3 * std::max(lmax, 1) * sizeof(double)));
+    double *soa = ctx->soa.as<double>();
+    double *rows[3];
+    for (int k = 0; k < 3; ++k) rows[k] = ctx->state.as<double>() + (size_t)k * chunk * std::max(lmax, 1);
+    const int npts_tab = 1000 * nmax;
+    const double2 *coef = ctx->coef.as<double2>();
+    // size the partial buffer once for the largest multipole of this call
+    {
+        size_t pmax = 0;
+        for (int l = 0; l < lmax; ++l) {
+            const int TILE = ((l + 1 > 32) || (nmax > 32)) ? 64 : 32;
+            const int mb = ceil_div(l + 1, TILE), nb = ceil_div(nmax, TILE);
+            int nslabs = std::min(std::max(1, (4 * ctx->sm_count) / (mb * nb)), ceil_div(chunk, kTP));
+            pmax = std::max(pmax, (size_t)nslabs * (l + 1) * nmax * sizeof(double2));
+        }
+        CG_CUDA_TRY(ctx->partial.ensure(pmax));
+    }
+    static bool attr_set = false;
+    if (!attr_set) {
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_fp64_raw_l<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(3 * kTP * (64 + 1) * sizeof(double))));
+        attr_set = true;
+    }
+
+    for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
+        const int64_t nc = std::min(chunk, npoints - c0);
+        double *r = soa, *x = soa + chunk, *ph = soa + 2 * chunk, *w = soa + 3 * chunk;
+        k_prep_points<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, weights_dev ? weights_dev + c0 : nullptr,
+                                                         nc, r, x, ph, w);
+        count_launch();
+        double *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
+        for (int l = 0; l < lmax; ++l) {
+            const bool big = (l + 1 > 32) || (nmax > 32);
+            const int TILE = big ? 64 : 32;
+            const int mb = ceil_div(l + 1, TILE), nb = ceil_div(nmax, TILE);
+            const int tiles = ceil_div(nc, kTP);
+            int nslabs = std::max(1, (4 * ctx->sm_count) / (mb * nb));
+            nslabs = std::min(nslabs, tiles);
+            LArgs a;
+            a.l = l;
+            a.nmax = nmax;
+            a.nslabs = nslabs;
+            a.n = nc;
+            a.r = r;
+            a.x = x;
+            a.ph = ph;
+            a.w = w;
+            a.kln = kln_dev + (size_t)l * nmax;
+            a.tab = interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr;
+            a.npts_tab = npts_tab;
+            a.dx_inv = interpolated ? ctx->tab_dxinv[l] : 0.0;
+            a.zmax = interpolated ? ctx->tab_zmax[l] : 0.0;
+            a.st1 = st1;
+            a.st2 = st2;
+            a.st0 = st0;
+            a.coef = coef + (size_t)l * (l + 1) / 2 * 1;  // (a,b) pairs: row l starts at l(l+1)/2 pairs
+            a.partial = ctx->partial.as<double2>();
+            a.err = err_dev;
+            dim3 grid(nslabs, mb, nb);
+            if (big) {
+                const size_t sm = 3 * kTP * (64 + 1) * sizeof(double);
+                k_fp64_raw_l<64><<<grid, kThreads, sm, st>>>(a);
+            } else {
+                const size_t sm = 3 * kTP * (32 + 1) * sizeof(double);
+                k_fp64_raw_l<32><<<grid, kThreads, sm, st>>>(a);
+            }
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            const int cnt = (l + 1) * nmax;
+            double2 *fl = reinterpret_cast<double2 *>(f_acc_dev) + (size_t)nmax * l * (l + 1) / 2;
+            k_sum_partials<<<ceil_div(cnt, 256), 256, 0, st>>>(ctx->partial.as<double2>(), nslabs, cnt, fl);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            // rotate rows: new l-1 <- st0, new l-2 <- st1
+            double *t = st2;
+            st2 = st1;
+            st1 = st0;
+            st0 = t;
+        }
+    }
+    return CATANA_OK;
+}
+
+catana_status_t finish_flmn_cln(double *f_dev, double norm, int lmax, int nmax, double *c_ln_dev, cudaStream_t st) {
+    const int cnt = lmax * nmax;
+    if (cnt == 0) return CATANA_OK;
+    k_finish<<<ceil_div(cnt, 128), 128, 0, st>>>(reinterpret_cast<double2 *>(f_dev), norm, lmax, nmax, c_ln_dev);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    return CATANA_OK;
+}
+
+}  // namespace catana_gpu

@@ -1,0 +1,164 @@
+"""sfb_decomposition and KClkk -- the decomposition module of the reference's
+Python API (python/py_decomposition.cpp), over the C ABI of libcatana_gpu.
+
+``sfb_decomposition(point_container, lmax, nmax, rmax, store_flmn=False,
+verbose=True)`` is the raw (direct-sum) method (py_decomposition.cpp:114-133,
+sfb_decomposition.cpp:15-19); called with a ``PixelizedPointContainer`` it is the
+HEALPix method (py_decomposition.cpp:135-153, sfb_decomposition.cpp:22-26).
+``sfb_decomposition_healpix`` is an alias of the second form.
+
+Keyword extensions (absent in the reference, defaults reproduce it):
+  weights=None         per-point weights; f is normalised by V/sum(w)
+  precision='plain'    'plain': FP64 on CUDA cores (the drop-in);
+                       'split': tcgen05 tensor cores, 3-term FP16 hi+lo products
+  interpolation='auto' 'auto' (interpolated iff N > 1000, the reference's rule),
+                       'on' (linear table) or 'off' (exact j_l)
+  conj_fix=False       HEALPix only: conjugate aliased ring coefficients instead of
+                       reproducing the reference's unconjugated read.
+"""
+import sys
+import time
+
+import numpy as np
+
+from . import _lib
+from .basictypes import PixelizedPointContainer, PointContainer
+
+_INTERP = {"auto": _lib.JL_AUTO, "on": _lib.JL_INTERP, "off": _lib.JL_EXACT}
+_FORM = {"plain": _lib.FORM_PLAIN, "split": _lib.FORM_SPLIT}
+
+
+class KClkk(object):
+    """Return type of the SFB decomposition methods (return_types.hpp:19-38).
+
+    k_ln, c_ln: (lmax, nmax) float64, read-only.  f_lmn: list over l of (l+1, nmax)
+    complex128 arrays (empty unless store_flmn).
+    """
+
+    def __init__(self, k_ln, c_ln, f_lmn):
+        k_ln.setflags(write=False)
+        c_ln.setflags(write=False)
+        self._k, self._c, self._f = k_ln, c_ln, f_lmn
+
+    @property
+    def k_ln(self):
+        return self._k
+
+    @property
+    def c_ln(self):
+        return self._c
+
+    @property
+    def f_lmn(self):
+        return self._f
+
+    def savetxt(self, filename_base):
+        """Write filename_base + '.k_ln' and '.c_ln' (rows l, columns n), '%.18e'
+        separated by single spaces (return_types.cpp:27-64)."""
+        for suffix, arr in ((".k_ln", self._k), (".c_ln", self._c)):
+            with open(filename_base + suffix, "w") as fh:
+                for row in arr:
+                    fh.write(" ".join("%.18e" % v for v in row) + "\n")
+
+
+def _unsigned_short(v, name):
+    if isinstance(v, bool) or not isinstance(v, (int, np.integer)) or not (0 <= int(v) <= 65535):
+        raise TypeError("%s must be an integer in [0, 65535] (C++ unsigned short)" % name)
+    return int(v)
+
+
+def unpack_flmn(flat, lmax, nmax):
+    """Split the packed complex f_lmn buffer into the list of (l+1, nmax) arrays."""
+    out, off = [], 0
+    for l in range(lmax):
+        s = (l + 1) * nmax
+        out.append(flat[off:off + s].reshape(l + 1, nmax).copy())
+        off += s
+    return out
+
+
+def _flags(interpolation, precision):
+    if interpolation not in _INTERP:
+        raise ValueError("interpolation must be one of %s" % sorted(_INTERP))
+    if precision not in _FORM:
+        raise ValueError("precision must be one of %s" % sorted(_FORM))
+    return _INTERP[interpolation] | _FORM[precision]
+
+
+def _raw(pc, lmax, nmax, rmax, store_flmn, verbose, weights, precision, interpolation):
+    pts = np.ascontiguousarray(np.asarray(pc, dtype=np.float64).reshape(-1, 3))
+    n = pts.shape[0]
+    w = None
+    if weights is not None:
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        if w.shape[0] != n:
+            raise ValueError("weights must have one entry per point")
+    if verbose:
+        print("SFB decomposition (raw method): lmax=%d nmax=%d Rmax=%s" % (lmax, nmax, rmax))
+        print("Catalog consists of %d points." % n)
+        sys.stdout.flush()
+    t0 = time.perf_counter()
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    fsize = int(_lib.lib.catana_gpu_flmn_size(lmax, nmax))
+    f = np.zeros(fsize, dtype=np.complex128) if store_flmn else None
+    st = _lib.lib.catana_gpu_sfb_raw(_lib.ptr(pts), _lib.ptr(w), n, lmax, nmax, float(rmax),
+                                     _flags(interpolation, precision), _lib.ptr(k), _lib.ptr(c), _lib.ptr(f), None)
+    _lib.check(st, "sfb_raw")
+    if verbose:
+        print("Done (%.3f s)." % (time.perf_counter() - t0))
+    return KClkk(k, c, unpack_flmn(f, lmax, nmax) if store_flmn else [])
+
+
+def _healpix(ppc, lmax, nmax, rmax, store_flmn, verbose, interpolation, conj_fix):
+    if verbose:
+        print("SFB decomposition (reverse method): lmax=%d nmax=%d NSide=%d" % (lmax, nmax, ppc.nside))
+        print("Catalog consists of %d points." % ppc.get_npoints())
+        sys.stdout.flush()
+    t0 = time.perf_counter()
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    fsize = int(_lib.lib.catana_gpu_flmn_size(lmax, nmax))
+    f = np.zeros(fsize, dtype=np.complex128) if store_flmn else None
+    flags = _flags(interpolation, "plain") | (_lib.HEALPIX_CONJ_FIX if conj_fix else 0)
+    rs = ppc.r_sorted if ppc.r_sorted.size else np.zeros(1)
+    st = _lib.lib.catana_gpu_sfb_healpix(ppc.nside, _lib.ptr(ppc.offsets), _lib.ptr(rs), lmax, nmax, float(rmax),
+                                         flags, _lib.ptr(k), _lib.ptr(c), _lib.ptr(f), None)
+    _lib.check(st, "sfb_healpix")
+    if verbose:
+        print("Done (%.3f s)." % (time.perf_counter() - t0))
+    return KClkk(k, c, unpack_flmn(f, lmax, nmax) if store_flmn else [])
+
+
+def sfb_decomposition(point_container, lmax, nmax, rmax, store_flmn=False, verbose=True, weights=None,
+                      precision="plain", interpolation="auto", conj_fix=False):
+    """Compute the SFB transform of a PointContainer (raw method) or of a
+    PixelizedPointContainer (HEALPix method).  Returns a KClkk."""
+    lmax = _unsigned_short(lmax, "lmax")
+    nmax = _unsigned_short(nmax, "nmax")
+    rmax = float(rmax)
+    if isinstance(point_container, PixelizedPointContainer):
+        if weights is not None or precision != "plain":
+            raise ValueError("the HEALPix method takes no weights and runs in FP64 only")
+        return _healpix(point_container, lmax, nmax, rmax, store_flmn, verbose, interpolation, conj_fix)
+    if not isinstance(point_container, PointContainer):
+        raise TypeError("sfb_decomposition expects a PointContainer or a PixelizedPointContainer")
+    return _raw(point_container, lmax, nmax, rmax, store_flmn, verbose, weights, precision, interpolation)
+
+
+def sfb_decomposition_healpix(pixelized_point_container, lmax, nmax, rmax, store_flmn=False, verbose=True,
+                              interpolation="auto", conj_fix=False):
+    """Alias of sfb_decomposition for a PixelizedPointContainer."""
+    if not isinstance(pixelized_point_container, PixelizedPointContainer):
+        raise TypeError("sfb_decomposition_healpix expects a PixelizedPointContainer")
+    return sfb_decomposition(pixelized_point_container, lmax, nmax, rmax, store_flmn, verbose,
+                             interpolation=interpolation, conj_fix=conj_fix)
+
+
+def compute_kln(lmax, nmax, rmax):
+    """k_ln = z_{l,n} / rmax (return_types.cpp:10-20), as a (lmax, nmax) array."""
+    lmax = _unsigned_short(lmax, "lmax")
+    nmax = _unsigned_short(nmax, "nmax")
+    k = np.zeros((lmax, nmax))
+    _lib.check(_lib.lib.catana_gpu_compute_kln(lmax, nmax, float(rmax), _lib.ptr(k)), "compute_kln")
+    return k

@@ -1,0 +1,146 @@
+/*
+ * catana_gpu.h -- C ABI of the GB300 (sm_103a) SFB decomposition library
+ * (libcatana_gpu.so).
+ *
+ * Plain pointers and sizes only; every entry point returns a catana_status_t and
+ * never throws.  Host-buffer entry points block until their results are in the
+ * caller's buffers; the *_dev entry points take device pointers and only enqueue
+ * work on the given stream (NULL = the legacy default stream).  The library keeps
+ * one context per device (workspace, cached Bessel-zero and coefficient tables);
+ * calls on one device are serialised by a mutex.
+ *
+ * Reference interfaces replaced (CatAna, paths relative to its repository):
+ *   catana::sfb_decomposition(const PointContainer&, ...)   sfb_decomposition.hpp:29-30,
+ *                                                            sfb_decomposition.cpp:15-19
+ *   catana::_sfb_raw(...)                                    sfb_raw.hpp:11-12, sfb_raw.cpp:13-108
+ *   catana::sfb_decomposition(const PixelizedPointContainer&, ...)
+ *                                                            sfb_decomposition.hpp:46-47,
+ *                                                            sfb_decomposition.cpp:22-26
+ *   catana::_sfb_reverse_fft(...)                            sfb_reverse_fft.hpp, sfb_reverse_fft.cpp:43-172
+ *   PixelizedPointContainer(nside, const PointContainer&)    PixelizedPointContainer.cpp:11-30
+ *   catana::compute_kln / KClkk::KClkk                        return_types.cpp:10-23
+ *   besseltools::SphericalBesselZeros::operator[]             SphericalBesselZeros.cpp:11-100
+ */
+#ifndef CATANA_GPU_H
+#define CATANA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t.  NULL selects the legacy default stream. */
+typedef struct CUstream_st *catana_gpu_stream_t;
+
+typedef enum {
+    CATANA_OK = 0,
+    CATANA_ERR_ARG = 1,         /* invalid argument (reference: std::invalid_argument -> ValueError) */
+    CATANA_ERR_DOMAIN = 2,      /* j_l argument at or beyond the interpolation table's end
+                                   (reference: std::domain_error -> ValueError) */
+    CATANA_ERR_CUDA = 3,        /* CUDA runtime error; see catana_gpu_last_error() */
+    CATANA_ERR_NOMEM = 4,       /* device or pinned allocation failed */
+    CATANA_ERR_UNSUPPORTED = 5  /* the requested form needs a device this build does not target */
+} catana_status_t;
+
+/* ---- flags for the SFB entry points ------------------------------------ */
+/* j_l evaluation.  AUTO is the reference's rule (sfb_decomposition.cpp:17,24):
+ * interpolate iff the catalog holds more than 1000 points. */
+#define CATANA_JL_AUTO 0u
+#define CATANA_JL_INTERP 1u  /* linear table, 1000*nmax nodes up to z_{l,nmax} (SBesselInterpolator.cpp:10-26) */
+#define CATANA_JL_EXACT 2u   /* direct j_l evaluation (the reference's gsl_sf_bessel_jl branch) */
+#define CATANA_JL_MASK 3u
+/* Contraction form.  PLAIN: FP64 on CUDA cores, the drop-in.  SPLIT: tensor-core
+ * tcgen05 contraction of 3-term FP16 hi+lo products with FP32 accumulation,
+ * FP64 across point chunks; j_l from a piecewise-cubic table accurate to ~1e-8
+ * (the JL flags do not apply). */
+#define CATANA_FORM_PLAIN 0u
+#define CATANA_FORM_SPLIT 4u
+#define CATANA_FORM_MASK 4u
+/* HEALPix path: 0 reproduces the reference's m-extraction, which reads
+ * F[rpix - m%rpix] without conjugation when m%rpix > rpix/2
+ * (sfb_reverse_fft.cpp:192-207); this flag conjugates it (the correct alias). */
+#define CATANA_HEALPIX_CONJ_FIX 8u
+
+/* ---- output layout -------------------------------------------------------
+ * k_ln, c_ln: lmax x nmax, row-major (index l*nmax + n) -- the numpy view of the
+ *             reference's KClkk.k_ln / c_ln (Eigen arrays exported to numpy).
+ * f_lmn:      complex128 as interleaved (re, im) doubles, packed by l: the block of
+ *             multipole l starts at complex index nmax*l*(l+1)/2 and holds the
+ *             (l+1) x nmax row-major array f[l][m][n], m = 0..l (KClkk.f_lmn[l]).
+ *             Total complex entries: catana_gpu_flmn_size(lmax, nmax).
+ */
+size_t catana_gpu_flmn_size(uint16_t lmax, uint16_t nmax);
+
+/* Raw (direct-sum) SFB decomposition of a point catalog.
+ *   f_lmn = sqrt(2/pi) * V/W * sum_i w_i k_ln j_l(k_ln r_i) Y*_lm(theta_i, phi_i),
+ *   V = 4/3 pi rmax^3, W = sum_i w_i (= N without weights),
+ *   C_ln  = sum_{m=-l..l} |f_l|m|n|^2 / (2l+1).
+ * points: npoints x 3 row-major (r, theta, phi), host memory (the PointContainer
+ *         buffer, py_basictypes.cpp:126-135).
+ * weights: optional per-point weights (NULL = unit weights; an extension -- the
+ *         reference's Point carries none).
+ * k_ln, c_ln: host, lmax*nmax doubles.  f_lmn: host or NULL.
+ * Replaces sfb_decomposition(const PointContainer&, lmax, nmax, rmax, store_flmn,
+ * verbose) and _sfb_raw (sfb_raw.cpp:13-108). */
+catana_status_t catana_gpu_sfb_raw(const double *points, const double *weights, int64_t npoints, uint16_t lmax,
+                                   uint16_t nmax, double rmax, uint32_t flags, double *k_ln, double *c_ln,
+                                   double *f_lmn, catana_gpu_stream_t stream);
+
+/* Same computation on device-resident data: all pointers are device pointers,
+ * the work is enqueued on `stream` and the call returns without synchronising
+ * except where a domain check needs the host (JL_INTERP); *status_dev (device
+ * int, may be NULL) receives CATANA_ERR_DOMAIN when an argument left the table. */
+catana_status_t catana_gpu_sfb_raw_dev(const double *points_dev, const double *weights_dev, int64_t npoints,
+                                       uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags,
+                                       double *k_ln_dev, double *c_ln_dev, double *f_lmn_dev,
+                                       int *status_dev, catana_gpu_stream_t stream);
+
+/* HEALPix (pixelized) SFB decomposition.  The catalog is given binned: pixel p
+ * (RING scheme) holds the radii r_sorted[pix_offsets[p] .. pix_offsets[p+1]), in
+ * the order the points were added.  npix = 12 nside^2; pix_offsets has npix+1
+ * entries.  Host pointers.  Replaces sfb_decomposition(const
+ * PixelizedPointContainer&, ...) and _sfb_reverse_fft (sfb_reverse_fft.cpp:43-209). */
+catana_status_t catana_gpu_sfb_healpix(int64_t nside, const int64_t *pix_offsets, const double *r_sorted,
+                                       uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags, double *k_ln,
+                                       double *c_ln, double *f_lmn, catana_gpu_stream_t stream);
+
+/* Bin a catalog into RING pixels: the PixelizedPointContainer(nside, pc)
+ * constructor (PixelizedPointContainer.cpp:11-30).  points: host npoints x 3
+ * (r, theta, phi).  Outputs (host): pix_offsets[npix+1] and r_sorted[npoints],
+ * radii grouped by pixel in point order.  nside must be a power of two
+ * (CATANA_ERR_ARG otherwise, like the reference); theta outside [0, pi] is
+ * CATANA_ERR_ARG (HEALPix asserts there). */
+catana_status_t catana_gpu_bin_points(int64_t nside, const double *points, int64_t npoints, int64_t *pix_offsets,
+                                      double *r_sorted, catana_gpu_stream_t stream);
+
+/* HEALPix RING ang2pix for n angles (host arrays in, host array out):
+ * Healpix_Base::ang2pix(pointing) as used at PixelizedPointContainer.cpp:28. */
+catana_status_t catana_gpu_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,
+                                        int64_t *pix, catana_gpu_stream_t stream);
+
+/* HEALPix RING pix2ang for n pixel indices: Healpix_Base::pix2ang as used at
+ * PixelizedPointContainer.cpp:17-19 (pixel centres). */
+catana_status_t catana_gpu_pix2ang_ring(int64_t nside, const int64_t *pix, int64_t n, double *theta, double *phi,
+                                        catana_gpu_stream_t stream);
+
+/* Zeros 0..count-1 of j_l, computed on the host exactly as
+ * besseltools::SphericalBesselZeros (SphericalBesselZeros.cpp:11-100), including
+ * its Newton stopping rule.  Cached per process. */
+catana_status_t catana_gpu_sbessel_zeros(uint32_t l, int32_t count, double *out);
+
+/* k_ln = z_{l,n} / rmax for l < lmax, n < nmax, row-major (return_types.cpp:10-20). */
+catana_status_t catana_gpu_compute_kln(uint16_t lmax, uint16_t nmax, double rmax, double *k_ln);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *catana_gpu_last_error(void);
+
+/* Number of kernel launches the library issued since process start (all devices). */
+uint64_t catana_gpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CATANA_GPU_H */

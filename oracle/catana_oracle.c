@@ -1,0 +1,646 @@
+/*
+ * catana_oracle.c -- CPU restatement of CatAna's spherical Fourier-Bessel (SFB)
+ * decomposition hot path.
+ *
+ * THIS FILE IS TEST INFRASTRUCTURE (the oracle). Only the test-suite, the smoke
+ * check and the CPU-baseline leg of bench.py load it, and only as the checker or
+ * as the timed CPU reference. The product library (catana_gb300) never links,
+ * imports or calls anything here.
+ *
+ * Parity pinning: the reference (CatAna) cannot be built in this environment
+ * (GSL, FFTW3, Eigen, HEALPix C++ and CFITSIO are absent and its submodules are
+ * empty).  This restatement follows the reference's algorithm step by step (file
+ * and line cited at every function) and is pinned by
+ *   - the reference's golden vectors test/test_data/gaussian_catalog.{python,
+ *     pythonrev}.{c_ln,k_ln} (rtol 1e-2 on C_ln, allclose on k_ln, exactly the
+ *     tolerance of test/python/decomposition_test.py:15-73);
+ *   - the reference's known answers (Bessel zeros, interpolator accuracy, point
+ *     conversion, HEALPix count maps);
+ *   - a bit-for-bit comparison of the zero finder and the interpolation table
+ *     against the reference's own SphericalBesselZeros.cpp / FunctionInterpolator.cpp
+ *     / SBesselInterpolator.cpp compiled from the reference tree against a GSL
+ *     shim whose j_l is the function below (oracle/Makefile, target `ref`);
+ *   - scipy/mpmath for the special functions (spherical_jn, sph_legendre_p).
+ * GSL's gsl_sf_bessel_jl and gsl_sf_legendre_sphPlm are replaced by published
+ * algorithms (DLMF 10.51, 10.53, 10.74 for j_l; DLMF 14.10 for the normalised
+ * associated Legendre recurrence) accurate to ~1e-15 relative.
+ *
+ * All entry points are plain C with an OpenMP parallel loop over points, in the
+ * same loop order as the reference: per multipole l, every point evaluates
+ * j_l(k_ln r) for all n, then P_lm for every m <= l from scratch (O(l-m) each,
+ * like gsl_sf_legendre_sphPlm), then accumulates k*j*Y*.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define CO_PI 3.14159265358979323846264338327950288
+
+/* ------------------------------------------------------------------------- */
+/* Spherical Bessel function j_l(x), FP64.                                   */
+/* Replaces gsl_sf_bessel_jl (called at sfb_raw.cpp:51,                      */
+/* SphericalBesselZeros.cpp:54-55, SBesselInterpolator.cpp:16).              */
+/* ------------------------------------------------------------------------- */
+
+/* Ascending series, DLMF 10.53.1: j_l(x) = x^l/(2l+1)!! * sum_k (-x^2/2)^k /
+ * (k! (2l+3)(2l+5)...(2l+2k+1)). */
+static double co_jl_series(int l, double x)
+{
+    double pre = 1.0;
+    for (int i = 1; i <= l; ++i) pre *= x / (2.0 * i + 1.0);
+    double hx2 = 0.5 * x * x;
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k < 200; ++k) {
+        term *= -hx2 / ((double)k * (2.0 * l + 2.0 * k + 1.0));
+        sum += term;
+        if (fabs(term) < 1e-17 * fabs(sum)) break;
+    }
+    return pre * sum;
+}
+
+/* Upward recurrence, DLMF 10.51.1, stable while l <= x. */
+static double co_jl_upward(int l, double x)
+{
+    double s = sin(x), c = cos(x);
+    double j0 = s / x;
+    if (l == 0) return j0;
+    double j1 = (j0 - c) / x;
+    for (int k = 1; k < l; ++k) {
+        double j2 = (2.0 * k + 1.0) / x * j1 - j0;
+        j0 = j1;
+        j1 = j2;
+    }
+    return j1;
+}
+
+/* Miller's backward recurrence (DLMF 3.6(vi), 10.74(iii)), normalised with the
+ * closed forms of j_0 or j_1, whichever is larger in magnitude. */
+static double co_jl_miller(int l, double x)
+{
+    double big = (double)l > x ? (double)l : x;
+    int nstart = (int)(big + 20.0 + 16.0 * cbrt(big + 1.0));
+    double jp1 = 0.0, jk = 1e-200, jl = 0.0;
+    if (nstart == l) jl = jk;
+    for (int k = nstart; k > 0; --k) {
+        double jm1 = (2.0 * k + 1.0) / x * jk - jp1;
+        jp1 = jk;
+        jk = jm1;
+        if (k - 1 == l) jl = jk;
+        if (fabs(jk) > 1e200) {
+            jk *= 1e-200;
+            jp1 *= 1e-200;
+            jl *= 1e-200;
+        }
+    }
+    /* jk = j_0 (unnormalised), jp1 = j_1 (unnormalised) */
+    double s = sin(x), c = cos(x);
+    double t0 = s / x;
+    double t1 = (t0 - c) / x;
+    if (fabs(t0) >= fabs(t1))
+        return jl * (t0 / jk);
+    return jl * (t1 / jp1);
+}
+
+double co_sbessel_jl(int l, double x)
+{
+    if (x == 0.0) return l == 0 ? 1.0 : 0.0;
+    if (x < 0.0) { /* j_l(-x) = (-1)^l j_l(x) */
+        double v = co_sbessel_jl(l, -x);
+        return (l & 1) ? -v : v;
+    }
+    if (x * x < 2.0 * l + 3.0) return co_jl_series(l, x);
+    if (x >= (double)l) return co_jl_upward(l, x);
+    return co_jl_miller(l, x);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Normalised associated Legendre function with Condon-Shortley phase,       */
+/* sqrt((2l+1)/(4pi) (l-m)!/(l+m)!) P_l^m(x): the quantity                   */
+/* gsl_sf_legendre_sphPlm returns (sfb_raw.cpp:73, sfb_reverse_fft.cpp:119). */
+/* Recurrence in l at fixed m, DLMF 14.10.3 in normalised form.              */
+/* ------------------------------------------------------------------------- */
+double co_sph_plm(int l, int m, double x)
+{
+    double somx2 = sqrt((1.0 - x) * (1.0 + x));
+    double pmm = 1.0 / sqrt(4.0 * CO_PI);
+    for (int i = 1; i <= m; ++i)
+        pmm *= -sqrt((2.0 * i + 1.0) / (2.0 * i)) * somx2;
+    if (l == m) return pmm;
+    double p1 = x * sqrt(2.0 * m + 3.0) * pmm;
+    if (l == m + 1) return p1;
+    double p2 = pmm;
+    double mm = (double)m * (double)m;
+    for (int ll = m + 2; ll <= l; ++ll) {
+        double dl = (double)ll, dl1 = (double)(ll - 1);
+        double a = sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+        double b = sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
+        double p = a * (x * p1 - b * p2);
+        p2 = p1;
+        p1 = p;
+    }
+    return p1;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Zeros of j_l: SphericalBesselZeros.cpp:11-68.                             */
+/* First two zeros from the asymptotic guesses (:17-47), Newton with the     */
+/* reference's stopping rule `while (delta/z > 1e-15)` (:49-62), which ends  */
+/* the loop after any negative step; further zeros start from the linear     */
+/* extrapolation 2 z_{n-1} - z_{n-2} (:64-68).                               */
+/* ------------------------------------------------------------------------- */
+static double co_newton(unsigned int l, double z)
+{
+    double delta, jl;
+    do {
+        jl = co_sbessel_jl((int)l, z);
+        delta = jl / ((double)l / z * jl - co_sbessel_jl((int)l + 1, z));
+        z -= delta;
+    } while (delta / z > 1e-15);
+    return z;
+}
+
+/* out[0..count) = zeros 0..count-1 of j_l, in the reference's order. */
+void co_sbessel_zeros(unsigned int l, int count, double *out)
+{
+    double z0, z1;
+    if (l == 0) {
+        z0 = 3.141592653589793238463;
+        z1 = 6.283185307179586476925;
+    } else {
+        double lh = l + 0.5;
+        z0 = l + 0.5 + 1.8557571 * pow(lh, 1. / 3.) + 1.033150 * pow(lh, -1. / 3.) - 0.00397 * pow(lh, -1.) -
+             0.0908 * pow(lh, -5. / 3.) + 0.043 * pow(lh, -7. / 3.);
+        z1 = l + 0.5 + 3.2446076 * pow(lh, 1. / 3.) + 3.158244 * pow(lh, -1. / 3.) - 0.08331 * pow(lh, -1.) -
+             0.8437 * pow(lh, -5. / 3.) + 0.864 * pow(lh, -7. / 3.);
+    }
+    double zs[2];
+    zs[0] = co_newton(l, z0);
+    zs[1] = co_newton(l, z1);
+    for (int n = 0; n < count && n < 2; ++n) out[n] = zs[n];
+    double a = zs[0], b = zs[1];
+    for (int n = 2; n < count; ++n) {
+        double z = co_newton(l, 2 * b - a);
+        out[n] = z;
+        a = b;
+        b = z;
+    }
+}
+
+/* k_ln table: return_types.cpp:10-20, k_ln(l,n) = SBZ(l)[n] / rmax.
+ * Output row-major [l][n] (lmax x nmax). */
+void co_compute_kln(int lmax, int nmax, double rmax, double *k_ln)
+{
+    double *z = (double *)malloc(sizeof(double) * (nmax > 2 ? nmax : 2));
+    for (int l = 0; l < lmax; ++l) {
+        co_sbessel_zeros((unsigned)l, nmax, z);
+        for (int n = 0; n < nmax; ++n) k_ln[(size_t)l * nmax + n] = z[n] / rmax;
+    }
+    free(z);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Linear interpolation table of j_l: SBesselInterpolator.cpp:10-26 and      */
+/* FunctionInterpolator.cpp:6-19. npts nodes x_i = 0 + i*dx on [0, zmax],     */
+/* dx = zmax/(npts-1), dx_inv = 1/dx, y_i = j_l(x_i).                         */
+/* ------------------------------------------------------------------------- */
+void co_lerp_table(int l, double zmax, int npts, double *y, double *dx_inv_out)
+{
+    double dx = (zmax - 0.0) / (npts - 1);
+    *dx_inv_out = 1. / dx;
+    for (int i = 0; i < npts; ++i) y[i] = co_sbessel_jl(l, 0.0 + (size_t)i * dx);
+}
+
+/* Evaluation: SBesselInterpolator.cpp:20-26.  Returns 0 and sets *err=1 when
+ * z >= zmax (the reference throws std::domain_error there). */
+static inline double co_lerp_eval(const double *y, int npts, double dx_inv, double zmax, double z, int *err)
+{
+    if (z >= zmax) {
+        *err = 1;
+        return 0.0;
+    }
+    double i_approx = z * dx_inv;
+    int i = (int)i_approx;
+    if (i > npts - 2) i = npts - 2; /* the reference would read y[npts] here */
+    return y[i] + (y[i + 1] - y[i]) * (i_approx - i);
+}
+
+double co_lerp_eval_pub(const double *y, int npts, double dx_inv, double zmax, double z, int *err)
+{
+    return co_lerp_eval(y, npts, dx_inv, zmax, z, err);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Raw SFB decomposition: sfb_raw.cpp:13-108 (+ the interpolation rule of    */
+/* sfb_decomposition.cpp:15-19 is chosen by the caller).                      */
+/*                                                                           */
+/* pts: N x 3 row-major (r, theta, phi) -- the PointContainer buffer layout   */
+/* (py_basictypes.cpp:126-135).  w: optional per-point weights (extension;    */
+/* with weights the normalisation uses V/sum(w) instead of V/N).              */
+/* Outputs: k_ln, c_ln row-major [l][n]; f_re/f_im (optional) packed by l,    */
+/* each l block (l+1) x nmax row-major [m][n].                                */
+/* Returns 0, or 2 when an argument left the interpolation range (the         */
+/* reference throws std::domain_error).                                       */
+/* ------------------------------------------------------------------------- */
+int co_sfb_raw(const double *pts, const double *w, int64_t npoints, int lmax, int nmax, double rmax,
+               int interpolated, int nthreads, double *k_ln, double *c_ln, double *f_re, double *f_im)
+{
+    if (nthreads <= 0) {
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#else
+        nthreads = 1;
+#endif
+    }
+    double wsum = (double)npoints;
+    if (w) {
+        wsum = 0.0;
+        for (int64_t i = 0; i < npoints; ++i) wsum += w[i];
+    }
+    /* sfb_raw.cpp:29-30 */
+    double norm_factor = sqrt(2. / CO_PI) * (4. / 3.) * CO_PI;
+    norm_factor *= rmax * rmax * rmax / wsum;
+
+    co_compute_kln(lmax, nmax, rmax, k_ln);
+    memset(c_ln, 0, sizeof(double) * (size_t)lmax * nmax);
+
+    int npts_tab = 1000 * nmax; /* BESSELINTERPOLATIONPOINTS_PER_ZERO * nmax */
+    double *table = interpolated ? (double *)malloc(sizeof(double) * npts_tab) : NULL;
+    double *zl = (double *)malloc(sizeof(double) * (nmax + 1 > 2 ? nmax + 1 : 2));
+    int err_any = 0;
+
+    size_t fsize_max = (size_t)lmax * nmax;
+    double *acc = (double *)calloc((size_t)nthreads * 2 * fsize_max, sizeof(double));
+    double *fl = (double *)malloc(sizeof(double) * 2 * fsize_max);
+    size_t foff = 0;
+
+    for (int l = 0; l < lmax; ++l) {
+        double dx_inv = 0.0, zmax = 0.0;
+        if (interpolated) {
+            /* SBesselInterpolator_uptozero(l, nmax, 1000*nmax): zmax = SBZ(l)[nmax] */
+            co_sbessel_zeros((unsigned)l, nmax + 1, zl);
+            zmax = zl[nmax];
+            co_lerp_table(l, zmax, npts_tab, table, &dx_inv);
+        }
+        size_t fs = (size_t)(l + 1) * nmax;
+        memset(acc, 0, sizeof(double) * (size_t)nthreads * 2 * fs);
+#pragma omp parallel num_threads(nthreads) reduction(| : err_any)
+        {
+            int tid = 0;
+#ifdef _OPENMP
+            tid = omp_get_thread_num();
+#endif
+            double *are = acc + (size_t)tid * 2 * fs;
+            double *aim = are + fs;
+            double *jn = (double *)malloc(sizeof(double) * nmax);
+            int err = 0;
+            /* contiguous static chunks: thread-private sums combined in thread order */
+#pragma omp for schedule(static)
+            for (int64_t i = 0; i < npoints; ++i) {
+                double r = pts[3 * i + 0], theta = pts[3 * i + 1], phi = pts[3 * i + 2];
+                double wi = w ? w[i] : 1.0;
+                for (int n = 0; n < nmax; ++n) {
+                    double z = k_ln[(size_t)l * nmax + n] * r;
+                    jn[n] = interpolated ? co_lerp_eval(table, npts_tab, dx_inv, zmax, z, &err)
+                                         : co_sbessel_jl(l, z);
+                }
+                double ct = cos(theta);
+                for (int m = 0; m <= l; ++m) {
+                    double plm = co_sph_plm(l, m, ct);
+                    double yre = plm * cos(-m * phi);
+                    double yim = plm * sin(-m * phi);
+                    for (int n = 0; n < nmax; ++n) {
+                        double kj = k_ln[(size_t)l * nmax + n] * jn[n] * wi;
+                        are[(size_t)m * nmax + n] += kj * yre;
+                        aim[(size_t)m * nmax + n] += kj * yim;
+                    }
+                }
+            }
+            free(jn);
+            err_any |= err;
+        }
+        /* reduction over threads (the reference's omp critical, sfb_raw.cpp:81-84) */
+        for (size_t q = 0; q < fs; ++q) {
+            double sre = 0.0, sim = 0.0;
+            for (int t = 0; t < nthreads; ++t) {
+                sre += acc[(size_t)t * 2 * fs + q];
+                sim += acc[(size_t)t * 2 * fs + fs + q];
+            }
+            fl[q] = sre * norm_factor;
+            fl[fs + q] = sim * norm_factor;
+        }
+        /* C_ln: sfb_raw.cpp:91-96 */
+        for (int n = 0; n < nmax; ++n) {
+            double c = 0.0;
+            for (int m = -l; m <= l; ++m) {
+                int am = m < 0 ? -m : m;
+                double re = fl[(size_t)am * nmax + n], im = fl[fs + (size_t)am * nmax + n];
+                c += re * re + im * im;
+            }
+            c_ln[(size_t)l * nmax + n] = c / (2 * l + 1);
+        }
+        if (f_re && f_im) {
+            memcpy(f_re + foff, fl, sizeof(double) * fs);
+            memcpy(f_im + foff, fl + fs, sizeof(double) * fs);
+        }
+        foff += fs;
+    }
+    free(acc);
+    free(fl);
+    free(zl);
+    free(table);
+    return err_any ? 2 : 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* HEALPix RING scheme (nside a power of two), restated from Gorski et al.    */
+/* 2005, ApJ 622:759, section 4 and the HEALPix primer.  The reference calls  */
+/* Healpix_Base::ang2pix / pix2ang / get_ring_info_small                      */
+/* (PixelizedPointContainer.cpp:16-30, sfb_reverse_fft.cpp:78).               */
+/* ------------------------------------------------------------------------- */
+static double co_fmodulo(double v1, double v2)
+{
+    if (v1 >= 0) return (v1 < v2) ? v1 : fmod(v1, v2);
+    double tmp = fmod(v1, v2) + v2;
+    return (tmp == v2) ? 0. : tmp;
+}
+
+static int64_t co_isqrt(int64_t v)
+{
+    int64_t r = (int64_t)sqrt((double)v + 0.5);
+    while (r * r > v) --r;
+    while ((r + 1) * (r + 1) <= v) ++r;
+    return r;
+}
+
+/* theta in [0, pi]; returns -1 for theta outside that range (HEALPix asserts). */
+int64_t co_ang2pix_ring(int64_t nside, double theta, double phi)
+{
+    if (!(theta >= 0.0 && theta <= CO_PI)) return -1;
+    int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    int have_sth = (theta < 0.01) || (theta > 3.14159 - 0.01);
+    double z = cos(theta), sth = have_sth ? sin(theta) : 0.0;
+    double za = fabs(z);
+    double tt = co_fmodulo(phi * 0.63661977236758134308, 4.0); /* phi / (pi/2) in [0,4) */
+    if (za <= 2. / 3.) {
+        int64_t nl4 = 4 * nside;
+        double temp1 = nside * (0.5 + tt);
+        double temp2 = nside * z * 0.75;
+        int64_t jp = (int64_t)(temp1 - temp2);
+        int64_t jm = (int64_t)(temp1 + temp2);
+        int64_t ir = nside + 1 + jp - jm;
+        int64_t kshift = 1 - (ir & 1);
+        int64_t t1 = jp + jm - nside + kshift + 1 + nl4 + nl4;
+        int64_t ip = (t1 >> 1) & (nl4 - 1);
+        return ncap + (ir - 1) * nl4 + ip;
+    } else {
+        double tp = tt - (int64_t)tt;
+        double tmp = ((za < 0.99) || !have_sth) ? nside * sqrt(3 * (1 - za)) : nside * sth / sqrt((1. + za) / 3.);
+        int64_t jp = (int64_t)(tp * tmp);
+        int64_t jm = (int64_t)((1.0 - tp) * tmp);
+        int64_t ir = jp + jm + 1;
+        int64_t ip = (int64_t)(tt * ir);
+        if (ip >= 4 * ir) ip -= 4 * ir;
+        return (z > 0) ? 2 * ir * (ir - 1) + ip : npix - 2 * ir * (ir + 1) + ip;
+    }
+}
+
+void co_pix2ang_ring(int64_t nside, int64_t pix, double *theta, double *phi)
+{
+    int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    double fact2 = 4. / npix, fact1 = (nside << 1) * fact2;
+    double z, ph, sth = 0.0;
+    int have_sth = 0;
+    if (pix < ncap) {
+        int64_t iring = (1 + co_isqrt(1 + 2 * pix)) >> 1;
+        int64_t iphi = (pix + 1) - 2 * iring * (iring - 1);
+        double tmp = (iring * iring) * fact2;
+        z = 1.0 - tmp;
+        if (z > 0.99) {
+            sth = sqrt(tmp * (2.0 - tmp));
+            have_sth = 1;
+        }
+        ph = (iphi - 0.5) * (0.5 * CO_PI) / iring;
+    } else if (pix < (npix - ncap)) {
+        int64_t nl4 = 4 * nside, ip = pix - ncap;
+        int64_t tmp = ip / nl4;
+        int64_t iring = tmp + nside, iphi = ip - nl4 * tmp + 1;
+        double fodd = ((iring + nside) & 1) ? 1 : 0.5;
+        z = (2 * nside - iring) * fact1;
+        ph = (iphi - fodd) * CO_PI * 0.75 * fact1;
+    } else {
+        int64_t ip = npix - pix;
+        int64_t iring = (1 + co_isqrt(2 * ip - 1)) >> 1;
+        int64_t iphi = 4 * iring + 1 - (ip - 2 * iring * (iring - 1));
+        double tmp = (iring * iring) * fact2;
+        z = tmp - 1.0;
+        if (z < -0.99) {
+            sth = sqrt(tmp * (2.0 - tmp));
+            have_sth = 1;
+        }
+        ph = (iphi - 0.5) * (0.5 * CO_PI) / iring;
+    }
+    *theta = have_sth ? atan2(sth, z) : acos(z);
+    *phi = ph;
+}
+
+/* ring in [1, 4 nside - 1] */
+void co_ring_info(int64_t nside, int64_t ring, int64_t *startpix, int64_t *ringpix)
+{
+    int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    if (ring < nside) {
+        *ringpix = 4 * ring;
+        *startpix = 2 * ring * (ring - 1);
+    } else if (ring < 3 * nside) {
+        *ringpix = 4 * nside;
+        *startpix = ncap + (ring - nside) * 4 * nside;
+    } else {
+        int64_t nr = 4 * nside - ring;
+        *ringpix = 4 * nr;
+        *startpix = npix - 2 * nr * (nr + 1);
+    }
+}
+
+/* Bin points into RING pixels (PixelizedPointContainer.cpp:11-30): the output
+ * is CSR -- offsets[npix+1] and r values in point order within each pixel.
+ * Returns -1 on a theta outside [0, pi]. */
+int co_bin_points(int64_t nside, const double *pts, int64_t npoints, int64_t *offsets, double *r_sorted)
+{
+    int64_t npix = 12 * nside * nside;
+    int64_t *pix = (int64_t *)malloc(sizeof(int64_t) * (npoints > 0 ? npoints : 1));
+    for (int64_t p = 0; p <= npix; ++p) offsets[p] = 0;
+    for (int64_t i = 0; i < npoints; ++i) {
+        pix[i] = co_ang2pix_ring(nside, pts[3 * i + 1], pts[3 * i + 2]);
+        if (pix[i] < 0) {
+            free(pix);
+            return -1;
+        }
+        offsets[pix[i] + 1]++;
+    }
+    for (int64_t p = 0; p < npix; ++p) offsets[p + 1] += offsets[p];
+    int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * npix);
+    memcpy(fill, offsets, sizeof(int64_t) * npix);
+    for (int64_t i = 0; i < npoints; ++i) r_sorted[fill[pix[i]]++] = pts[3 * i];
+    free(fill);
+    free(pix);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* HEALPix SFB: sfb_reverse_fft.cpp:43-209.  Per (l, n): per ring, the map of  */
+/* summed j_l(k r) per pixel, its real DFT (FFTW r2c convention, F[s] =       */
+/* sum_j map_j exp(-2 pi i j s / rpix), s <= rpix/2), then the m-extraction   */
+/* with the reference's index mapping m_ = rpix/2 - |rpix/2 - (m % rpix)| and */
+/* sign = (m > 0): the imaginary part is never negated, so m > rpix/2 takes   */
+/* F[rpix - m%rpix] instead of its conjugate (sfb_reverse_fft.cpp:192-207).  */
+/* The DFT is evaluated directly for the frequencies the extraction reads.    */
+/* ------------------------------------------------------------------------- */
+int co_sfb_healpix(int64_t nside, const int64_t *offsets, const double *r_sorted, int lmax, int nmax, double rmax,
+                   int interpolated, int nthreads, double *k_ln, double *c_ln, double *f_re, double *f_im)
+{
+    if (nthreads <= 0) {
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#else
+        nthreads = 1;
+#endif
+    }
+    int64_t npix = 12 * nside * nside;
+    int64_t nrings = 4 * nside - 1;
+    int64_t npoints = offsets[npix];
+    double norm_factor = sqrt(2. / CO_PI) * (4. / 3.) * CO_PI;
+    norm_factor *= rmax * rmax * rmax / (double)npoints;
+    co_compute_kln(lmax, nmax, rmax, k_ln);
+    memset(c_ln, 0, sizeof(double) * (size_t)lmax * nmax);
+
+    int64_t *rstart = (int64_t *)malloc(sizeof(int64_t) * nrings);
+    int64_t *rpixv = (int64_t *)malloc(sizeof(int64_t) * nrings);
+    double *costh = (double *)malloc(sizeof(double) * nrings);
+    double *phase = (double *)malloc(sizeof(double) * nrings);
+    for (int64_t i = 0; i < nrings; ++i) {
+        co_ring_info(nside, i + 1, &rstart[i], &rpixv[i]);
+        double th, ph;
+        co_pix2ang_ring(nside, rstart[i], &th, &ph);
+        costh[i] = cos(th);
+        phase[i] = ph;
+    }
+    int npts_tab = 1000 * nmax;
+    double *table = interpolated ? (double *)malloc(sizeof(double) * npts_tab) : NULL;
+    double *zl = (double *)malloc(sizeof(double) * (nmax + 1 > 2 ? nmax + 1 : 2));
+    double *ylm = (double *)malloc(sizeof(double) * 2 * (size_t)nrings * lmax);
+    double *acc = (double *)malloc(sizeof(double) * 2 * (size_t)nthreads * lmax);
+    int err_any = 0;
+    size_t foff = 0;
+
+    for (int l = 0; l < lmax; ++l) {
+        double dx_inv = 0.0, zmax = 0.0;
+        if (interpolated) {
+            co_sbessel_zeros((unsigned)l, nmax + 1, zl);
+            zmax = zl[nmax];
+            co_lerp_table(l, zmax, npts_tab, table, &dx_inv);
+        }
+        for (int64_t i = 0; i < nrings; ++i)
+            for (int m = 0; m <= l; ++m) {
+                double p = co_sph_plm(l, m, costh[i]);
+                ylm[2 * (i * (l + 1) + m)] = p * cos(-m * phase[i]);
+                ylm[2 * (i * (l + 1) + m) + 1] = p * sin(-m * phase[i]);
+            }
+        size_t fs = (size_t)(l + 1) * nmax;
+        for (int n = 0; n < nmax; ++n) {
+            double k_n = k_ln[(size_t)l * nmax + n];
+            memset(acc, 0, sizeof(double) * 2 * (size_t)nthreads * (l + 1));
+#pragma omp parallel num_threads(nthreads) reduction(| : err_any)
+            {
+                int tid = 0;
+#ifdef _OPENMP
+                tid = omp_get_thread_num();
+#endif
+                double *a = acc + (size_t)tid * 2 * (l + 1);
+                int err = 0;
+                double *map = (double *)malloc(sizeof(double) * 4 * nside);
+#pragma omp for schedule(static)
+                for (int64_t i = 0; i < nrings; ++i) {
+                    int64_t rp = rpixv[i];
+                    for (int64_t j = 0; j < rp; ++j) {
+                        double s = 0.0;
+                        int64_t p = rstart[i] + j;
+                        for (int64_t q = offsets[p]; q < offsets[p + 1]; ++q) {
+                            double z = k_n * r_sorted[q];
+                            s += interpolated ? co_lerp_eval(table, npts_tab, dx_inv, zmax, z, &err)
+                                              : co_sbessel_jl(l, z);
+                        }
+                        map[j] = s;
+                    }
+                    for (int m = 0; m <= l; ++m) {
+                        int64_t mi = rp / 2 - (m % rp);
+                        int sign = (m > 0) - (m < 0);
+                        mi = rp / 2 - (mi < 0 ? -mi : mi);
+                        /* F[mi] by direct DFT */
+                        double fre = 0.0, fim = 0.0;
+                        for (int64_t j = 0; j < rp; ++j) {
+                            double ang = -2.0 * CO_PI * (double)((j * mi) % rp) / (double)rp;
+                            fre += map[j] * cos(ang);
+                            fim += map[j] * sin(ang);
+                        }
+                        fim *= sign;
+                        double yre = ylm[2 * (i * (l + 1) + m)], yim = ylm[2 * (i * (l + 1) + m) + 1];
+                        a[2 * m] += fre * yre - fim * yim;
+                        a[2 * m + 1] += fre * yim + fim * yre;
+                    }
+                }
+                free(map);
+                err_any |= err;
+            }
+            double sq = 0.0, f0 = 0.0;
+            for (int m = 0; m <= l; ++m) {
+                double sre = 0.0, sim = 0.0;
+                for (int t = 0; t < nthreads; ++t) {
+                    sre += acc[(size_t)t * 2 * (l + 1) + 2 * m];
+                    sim += acc[(size_t)t * 2 * (l + 1) + 2 * m + 1];
+                }
+                double a2 = sre * sre + sim * sim;
+                sq += a2;
+                if (m == 0) f0 = a2;
+                if (f_re && f_im) {
+                    f_re[foff + (size_t)m * nmax + n] = sre * k_n * norm_factor;
+                    f_im[foff + (size_t)m * nmax + n] = sim * k_n * norm_factor;
+                }
+            }
+            double c = 2 * sq - f0;
+            double nk = norm_factor * k_n;
+            c *= nk * nk / (2 * l + 1);
+            c_ln[(size_t)l * nmax + n] = c;
+        }
+        foff += fs;
+    }
+    free(rstart);
+    free(rpixv);
+    free(costh);
+    free(phase);
+    free(table);
+    free(zl);
+    free(ylm);
+    free(acc);
+    return err_any ? 2 : 0;
+}
+
+/* Point(x, y, z): Point.cpp:5-10 -- r = |v|, theta = atan2(rho, z),
+ * phi = atan2(y, x) reduced into [0, 2 pi) (HEALPix pointing(vec3) + normalize). */
+void co_cartesian_to_spherical(const double *xyz, int64_t n, double *rtp)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        double rho = sqrt(x * x + y * y);
+        double r = sqrt(x * x + y * y + z * z);
+        double th = atan2(rho, z);
+        double ph = (x == 0.0 && y == 0.0) ? 0.0 : atan2(y, x);
+        if (ph < 0.0) ph += 2.0 * CO_PI;
+        ph = co_fmodulo(ph, 2.0 * CO_PI);
+        rtp[3 * i] = r;
+        rtp[3 * i + 1] = th;
+        rtp[3 * i + 2] = ph;
+    }
+}

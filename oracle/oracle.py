@@ -1,0 +1,212 @@
+"""ctypes front-end of the CPU oracle (catana_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` as
+the checker, and by ``bench.py``'s CPU-baseline leg.  The product package
+(catana_gb300) never imports this module.
+
+Builds ``oracle/_build/libcatana_oracle.so`` with the Makefile beside it on first
+use when it is missing.  ``ref_lib()`` loads the reference's own besseltools
+sources compiled by ``make -C oracle ref`` (only possible where the reference
+tree exists); it returns None elsewhere.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libcatana_oracle.so")
+_REF_PATH = os.path.join(_HERE, "_ref", "libref_besseltools.so")
+_lib = None
+_ref = None
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_P = ctypes.c_void_p
+
+
+def build(force=False):
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
+
+
+def build_ref(ref_root="/root/reference"):
+    """Compile the reference's besseltools sources (needs the reference tree)."""
+    if not os.path.isdir(ref_root):
+        return False
+    subprocess.run(["make", "-s", "-C", _HERE, "ref", "REF=" + ref_root], check=True)
+    return True
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.co_sbessel_jl.restype = _D
+        L.co_sbessel_jl.argtypes = [_I, _D]
+        L.co_sph_plm.restype = _D
+        L.co_sph_plm.argtypes = [_I, _I, _D]
+        L.co_sbessel_zeros.restype = None
+        L.co_sbessel_zeros.argtypes = [ctypes.c_uint, _I, _P]
+        L.co_compute_kln.restype = None
+        L.co_compute_kln.argtypes = [_I, _I, _D, _P]
+        L.co_lerp_table.restype = None
+        L.co_lerp_table.argtypes = [_I, _D, _I, _P, _P]
+        L.co_lerp_eval_pub.restype = _D
+        L.co_lerp_eval_pub.argtypes = [_P, _I, _D, _D, _D, _P]
+        L.co_sfb_raw.restype = _I
+        L.co_sfb_raw.argtypes = [_P, _P, _I64, _I, _I, _D, _I, _I, _P, _P, _P, _P]
+        L.co_ang2pix_ring.restype = _I64
+        L.co_ang2pix_ring.argtypes = [_I64, _D, _D]
+        L.co_pix2ang_ring.restype = None
+        L.co_pix2ang_ring.argtypes = [_I64, _I64, _P, _P]
+        L.co_ring_info.restype = None
+        L.co_ring_info.argtypes = [_I64, _I64, _P, _P]
+        L.co_bin_points.restype = _I
+        L.co_bin_points.argtypes = [_I64, _P, _I64, _P, _P]
+        L.co_sfb_healpix.restype = _I
+        L.co_sfb_healpix.argtypes = [_I64, _P, _P, _I, _I, _D, _I, _I, _P, _P, _P, _P]
+        L.co_cartesian_to_spherical.restype = None
+        L.co_cartesian_to_spherical.argtypes = [_P, _I64, _P]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's SphericalBesselZeros/SBesselInterpolator, or None."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(_REF_PATH):
+            return None
+        R = ctypes.CDLL(_REF_PATH)
+        R.ref_sbessel_zeros.restype = None
+        R.ref_sbessel_zeros.argtypes = [ctypes.c_uint, _I, _P]
+        R.ref_interp_table.restype = None
+        R.ref_interp_table.argtypes = [ctypes.c_ushort, ctypes.c_ushort, ctypes.c_uint, _P, _P]
+        R.ref_interp_eval.restype = _I
+        R.ref_interp_eval.argtypes = [ctypes.c_ushort, ctypes.c_ushort, ctypes.c_uint, _P, _I, _P]
+        _ref = R
+    return _ref
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def sbessel_jl(l, x):
+    return lib().co_sbessel_jl(int(l), float(x))
+
+
+def sph_plm(l, m, x):
+    return lib().co_sph_plm(int(l), int(m), float(x))
+
+
+def sbessel_zeros(l, count):
+    out = np.zeros(count, dtype=np.float64)
+    lib().co_sbessel_zeros(int(l), int(count), _ptr(out))
+    return out
+
+
+def compute_kln(lmax, nmax, rmax):
+    out = np.zeros((lmax, nmax), dtype=np.float64)
+    lib().co_compute_kln(int(lmax), int(nmax), float(rmax), _ptr(out))
+    return out
+
+
+def lerp_table(l, zmax, npts):
+    y = np.zeros(npts, dtype=np.float64)
+    dxi = np.zeros(1, dtype=np.float64)
+    lib().co_lerp_table(int(l), float(zmax), int(npts), _ptr(y), _ptr(dxi))
+    return y, float(dxi[0])
+
+
+def cartesian_to_spherical(xyz):
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros_like(xyz)
+    lib().co_cartesian_to_spherical(_ptr(xyz), xyz.shape[0], _ptr(out))
+    return out
+
+
+def sfb_raw(pts, lmax, nmax, rmax, interpolated, weights=None, store_flmn=True, nthreads=0):
+    """Raw SFB decomposition (sfb_raw.cpp:13-108).
+
+    pts: (N, 3) float64 (r, theta, phi).  Returns (k_ln, c_ln, f_lmn) where f_lmn is
+    a list of complex128 (l+1, nmax) arrays (empty when store_flmn is False).
+    """
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    nf = nmax * lmax * (lmax + 1) // 2
+    fre = np.zeros(nf) if store_flmn else None
+    fim = np.zeros(nf) if store_flmn else None
+    rc = lib().co_sfb_raw(_ptr(pts), _ptr(w), pts.shape[0], int(lmax), int(nmax), float(rmax),
+                          int(bool(interpolated)), int(nthreads), _ptr(k), _ptr(c), _ptr(fre), _ptr(fim))
+    if rc == 2:
+        raise ValueError("argument (z) outside of defined range.")
+    return k, c, _unpack_f(fre, fim, lmax, nmax) if store_flmn else []
+
+
+def _unpack_f(fre, fim, lmax, nmax):
+    out, off = [], 0
+    for l in range(lmax):
+        s = (l + 1) * nmax
+        out.append((fre[off:off + s] + 1j * fim[off:off + s]).reshape(l + 1, nmax))
+        off += s
+    return out
+
+
+def ang2pix_ring(nside, theta, phi):
+    L = lib()
+    th = np.asarray(theta, dtype=np.float64).ravel()
+    ph = np.asarray(phi, dtype=np.float64).ravel()
+    return np.array([L.co_ang2pix_ring(int(nside), float(a), float(b)) for a, b in zip(th, ph)], dtype=np.int64)
+
+
+def pix2ang_ring(nside, pix):
+    L = lib()
+    t = np.zeros(1)
+    p = np.zeros(1)
+    th, ph = [], []
+    for q in np.asarray(pix).ravel():
+        L.co_pix2ang_ring(int(nside), int(q), _ptr(t), _ptr(p))
+        th.append(t[0])
+        ph.append(p[0])
+    return np.array(th), np.array(ph)
+
+
+def ring_info(nside, ring):
+    s = np.zeros(1, dtype=np.int64)
+    n = np.zeros(1, dtype=np.int64)
+    lib().co_ring_info(int(nside), int(ring), _ptr(s), _ptr(n))
+    return int(s[0]), int(n[0])
+
+
+def bin_points(nside, pts):
+    pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    npix = 12 * nside * nside
+    offs = np.zeros(npix + 1, dtype=np.int64)
+    rs = np.zeros(max(pts.shape[0], 1), dtype=np.float64)
+    rc = lib().co_bin_points(int(nside), _ptr(pts), pts.shape[0], _ptr(offs), _ptr(rs))
+    if rc != 0:
+        raise ValueError("theta outside [0, pi]")
+    return offs, rs[:pts.shape[0]]
+
+
+def sfb_healpix(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, store_flmn=True, nthreads=0):
+    """HEALPix SFB decomposition (sfb_reverse_fft.cpp:43-209)."""
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    r_sorted = np.ascontiguousarray(r_sorted, dtype=np.float64)
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    nf = nmax * lmax * (lmax + 1) // 2
+    fre = np.zeros(nf) if store_flmn else None
+    fim = np.zeros(nf) if store_flmn else None
+    rc = lib().co_sfb_healpix(int(nside), _ptr(offsets), _ptr(r_sorted), int(lmax), int(nmax), float(rmax),
+                              int(bool(interpolated)), int(nthreads), _ptr(k), _ptr(c), _ptr(fre), _ptr(fim))
+    if rc == 2:
+        raise ValueError("argument (z) outside of defined range.")
+    return k, c, _unpack_f(fre, fim, lmax, nmax) if store_flmn else []

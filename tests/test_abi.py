@@ -1,0 +1,125 @@
+"""CPU-side checks of the product: the C-ABI library loads and exports every symbol
+include/catana_gpu.h declares; host logic (Bessel zeros, argument validation,
+containers, KClkk.savetxt) behaves like the reference.  No GPU compute here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import catana_gb300 as catana
+from catana_gb300 import _lib
+from oracle import oracle as O
+from conftest import ROOT
+
+
+def _declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(catana_gpu_\w+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    names = _declared_symbols()
+    assert len(names) >= 10
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_flmn_size():
+    assert _lib.lib.catana_gpu_flmn_size(32, 32) == 32 * 32 * 33 // 2
+    assert _lib.lib.catana_gpu_flmn_size(0, 5) == 0
+
+
+def test_kln_matches_oracle_bitwise():
+    for lmax, nmax, rmax in [(10, 10, 2500.0), (32, 32, 1000.0), (64, 40, 777.0)]:
+        assert np.array_equal(catana.compute_kln(lmax, nmax, rmax), O.compute_kln(lmax, nmax, rmax))
+
+
+def test_spherical_bessel_zeros_api():
+    z = catana.besseltools.SphericalBesselZeros(0)
+    assert z[0] == pytest.approx(np.pi)
+    assert z[1] == pytest.approx(6.283185307179586)
+    assert z[2] == pytest.approx(9.42477796076938)
+    assert catana.besseltools.SphericalBesselZeros(5)[9] == pytest.approx(38.8836)
+    z2 = catana.besseltools.SphericalBesselZeros(2)
+    z2.compute_up_to(100)
+    with pytest.raises(TypeError):
+        catana.besseltools.SphericalBesselZeros()
+
+
+def test_point_api():
+    """point_test.py:5-17."""
+    p = catana.Point()
+    assert p.cartesian() == (0.0, 0.0, 0.0)
+    assert p.spherical() == (0.0, 0.0, 0.0)
+    assert np.allclose(p, np.zeros(3))
+    p = catana.Point(0, 0, 1)
+    assert p.spherical() == (1, 0, 0)
+    assert p.cartesian() == pytest.approx((0, 0, 1))
+
+
+def test_point_container_api():
+    """point_test.py:20-43 plus the constructor's error paths (py_basictypes.cpp:83-110)."""
+    pc = catana.PointContainer()
+    assert np.array(pc).shape == (0, 3)
+    pc.add_point(catana.Point())
+    assert np.array(pc).shape == (1, 3)
+    data = np.arange(9).reshape(3, 3)
+    assert np.allclose(catana.PointContainer(data), data)
+    pc = catana.PointContainer(np.ones((2, 3)))
+    assert np.allclose(pc[0], pc[1]) and np.allclose(pc[0], [1, 1, 1])
+    with pytest.raises(IndexError):
+        pc[2]
+    with pytest.raises(RuntimeError):
+        catana.PointContainer(np.ones((2, 3)), "polar")
+    with pytest.raises(RuntimeError):
+        catana.PointContainer(np.ones(3))
+    with pytest.raises(RuntimeError):
+        catana.PointContainer(np.ones((2, 4)))
+    with pytest.raises(RuntimeError):
+        catana.PointContainer(np.asfortranarray(np.ones((4, 3))))
+    xyz = np.array([[0, 0, 1], [1, 1, 1], [-380, -800, 200]], dtype=float)
+    assert np.allclose(np.array(catana.PointContainer(xyz, "cartesian")), O.cartesian_to_spherical(xyz), rtol=1e-15)
+
+
+def test_pixelized_container_host_side():
+    """point_test.py:46-53 and PixelizedPointContainer.cpp:13-15."""
+    with pytest.raises(TypeError):
+        catana.PixelizedPointContainer()
+    ppc = catana.PixelizedPointContainer(4)
+    assert np.all(ppc.get_countmap() == np.zeros(4 ** 2 * 12))
+    assert len(ppc) == 12 * 16
+    with pytest.raises(ValueError):
+        catana.PixelizedPointContainer(255)
+
+
+def test_sfb_argument_validation():
+    pc = catana.PointContainer(np.ones((3, 3)))
+    with pytest.raises(TypeError):
+        catana.sfb_decomposition(pc, -1, 4, 10.0)
+    with pytest.raises(TypeError):
+        catana.sfb_decomposition(pc, 4, 70000, 10.0)
+    with pytest.raises(TypeError):
+        catana.sfb_decomposition(np.ones((3, 3)), 4, 4, 10.0)
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition(pc, 4, 4, 10.0, precision="half")
+
+
+def test_savetxt_format(tmp_path):
+    k = np.array([[1.256637061435917236e-03, 2.5e-3]])
+    c = np.array([[1.0, 2.0]])
+    r = catana.KClkk(k.copy(), c.copy(), [])
+    base = str(tmp_path / "x")
+    r.savetxt(base)
+    line = open(base + ".k_ln").read().splitlines()[0]
+    assert line == "1.256637061435917236e-03 2.500000000000000052e-03"
+    assert np.array_equal(np.loadtxt(base + ".c_ln", ndmin=2), c)
+    with pytest.raises(ValueError):
+        r.k_ln[0, 0] = 1.0
