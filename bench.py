@@ -1,0 +1,354 @@
+"""Benchmark of the raw SFB decomposition (points*modes/s).
+
+Default workload: the split-precision raw SFB -- 10M points uniform in a ball of
+rmax=1000 (r = rmax u^(1/3), cos(theta) ~ U[-1,1], phi ~ U[0,2pi)), weights
+U[0.5,1.5] (float64), lmax=256, nmax=128, seed 2.  A "step" is one full
+decomposition of that catalog (f_lmn and C_ln for every l < lmax, n < nmax).
+modes = nmax * sum_{l<lmax} (l+1); the unit counts points * modes per second.
+
+value   device-resident inputs (points 240 MB + weights 80 MB, larger than L2),
+        device outputs, CUDA events on the launching stream, max over ranks.
+e2e     the same through the host-buffer C ABI (catana_gpu_sfb_raw): pinned host
+        input, host->device copy, compute, device->host copy of k_ln and C_ln.
+roofline  the dominant kernel (the tcgen05 contraction, k_split_l) timed with CUDA
+        events inside the timed region; algorithmic work = 4 flops per point-mode;
+        peak = measured dense bf16/fp16 burst peak / 3 (three hi/lo products per MAC).
+cpu_baseline  the oracle's OpenMP restatement of the reference's raw path on a
+        bounded point sample, all host cores, same lmax/nmax.
+
+--impl reference times only that CPU path (rank 0), a bounded sample per step.
+Multi-GPU (torchrun): every rank decomposes its own 10M-point shard of one catalog
+(weak scaling); the unnormalised f_lmn are summed with one NCCL all-reduce.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "raw SFB points·modes/s, split-precision vs FP64 plain, C_l err≤1e-6"
+UNIT = "point*modes/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--form", default="split", choices=["split", "plain"])
+    p.add_argument("--points", type=int, default=10_000_000)
+    p.add_argument("--lmax", type=int, default=256)
+    p.add_argument("--nmax", type=int, default=128)
+    p.add_argument("--rmax", type=float, default=1000.0)
+    p.add_argument("--seed", type=int, default=2)
+    p.add_argument("--cpu-sample", type=int, default=600, help="points in the CPU baseline sample")
+    p.add_argument("--plain-sample", type=int, default=100_000, help="points for the FP64 plain GPU comparison")
+    p.add_argument("--no-extras", action="store_true", help="skip e2e/cpu/plain/accuracy legs")
+    return p.parse_args()
+
+
+def catalog(n, rmax, seed, shard=0):
+    rng = np.random.default_rng([seed, shard])
+    r = rmax * rng.random(n) ** (1.0 / 3.0)
+    th = np.arccos(rng.uniform(-1.0, 1.0, n))
+    ph = rng.uniform(0.0, 2.0 * np.pi, n)
+    w = rng.uniform(0.5, 1.5, n)
+    return np.ascontiguousarray(np.stack([r, th, ph], axis=1)), w
+
+
+def modes(lmax, nmax):
+    return nmax * lmax * (lmax + 1) // 2
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["bf16_tflops"]), float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 6800.0, "fallback"
+
+
+def cpu_baseline(pts, w, lmax, nmax, rmax):
+    """The oracle's restatement of sfb_raw.cpp on a bounded sample, all host cores."""
+    from oracle import oracle as O
+    O.build()
+    t = time.perf_counter()
+    O.sfb_raw(pts, lmax, nmax, rmax, interpolated=True, weights=w, store_flmn=False)
+    dt = time.perf_counter() - t
+    return pts.shape[0] * modes(lmax, nmax) / dt, dt
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pts, w = catalog(a.cpu_sample, a.rmax, a.seed)
+    for _ in range(a.warmup):
+        cpu_baseline(pts, w, a.lmax, a.nmax, a.rmax)
+    t = time.perf_counter()
+    for _ in range(a.steps):
+        cpu_baseline(pts, w, a.lmax, a.nmax, a.rmax)
+    dt = (time.perf_counter() - t) / a.steps
+    v = a.cpu_sample * modes(a.lmax, a.nmax) / dt
+    cores = os.cpu_count()
+    sample = "%d of the %d points per step (same lmax/nmax/rmax/weights; the path is linear in N)" % (
+        a.cpu_sample, a.points)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(a),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def workload_config(a):
+    return {"workload": "raw SFB %s form: %d points uniform in a ball rmax=%g, weights U[0.5,1.5], lmax=%d, "
+                        "nmax=%d, seed %d" % (a.form, a.points, a.rmax, a.lmax, a.nmax, a.seed),
+            "points_per_gpu": a.points, "lmax": a.lmax, "nmax": a.nmax, "rmax": a.rmax,
+            "form": a.form, "modes": modes(a.lmax, a.nmax),
+            "l2": "inputs (%.0f MB) larger than L2 (129 MB); no flush" % (a.points * 32 / 1e6)}
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import torch
+    import catana_gb300 as catana  # noqa: F401
+    from catana_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    flags = _lib.FORM_SPLIT if a.form == "split" else (_lib.FORM_PLAIN | _lib.JL_AUTO)
+    L, M = a.lmax, a.nmax
+    nmodes = modes(L, M)
+    pts, w = catalog(a.points, a.rmax, a.seed, shard=rank)
+    h_pts = torch.from_numpy(pts).pin_memory()
+    h_w = torch.from_numpy(w).pin_memory()
+    d_pts = h_pts.cuda()
+    d_w = h_w.cuda()
+    fsz = int(_lib.lib.catana_gpu_flmn_size(L, M))
+    d_k = torch.zeros(L * M, dtype=torch.float64, device="cuda")
+    d_c = torch.zeros_like(d_k)
+    d_f = torch.zeros(2 * fsz, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        st = _lib.lib.catana_gpu_sfb_raw_dev(ctypes.c_void_p(d_pts.data_ptr()), ctypes.c_void_p(d_w.data_ptr()),
+                                             a.points, L, M, a.rmax, flags, ctypes.c_void_p(d_k.data_ptr()),
+                                             ctypes.c_void_p(d_c.data_ptr()), ctypes.c_void_p(d_f.data_ptr()),
+                                             None, sp)
+        _lib.check(st, "sfb_raw_dev")
+        if dist is not None:
+            # one catalog sharded over ranks: f_total = sum_r (N_r / N) f_r
+            d_f.mul_(1.0 / world)
+            dist.all_reduce(d_f)
+            fz = torch.view_as_complex(d_f.view(-1, 2))
+            off = 0
+            cl = []
+            for l in range(L):
+                blk = fz[off:off + (l + 1) * M].view(l + 1, M)
+                p = blk.real ** 2 + blk.imag ** 2
+                cl.append((2 * p.sum(0) - p[0]) / (2 * l + 1))
+                off += (l + 1) * M
+            d_c.copy_(torch.stack(cl).reshape(-1))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(a.warmup):
+        step()
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = int(_lib.lib.catana_gpu_launch_count())
+    _lib.lib.catana_gpu_profile_enable(1)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        step()
+    ev1.record(stream)
+    barrier()
+    _lib.lib.catana_gpu_profile_enable(0)
+    ms_total = ev0.elapsed_time(ev1)
+    launches = int(_lib.lib.catana_gpu_launch_count()) - launches0
+    kms = ctypes.c_double(0.0)
+    kn = ctypes.c_uint64(0)
+    kfl = ctypes.c_double(0.0)
+    _lib.check(_lib.lib.catana_gpu_profile_report(ctypes.byref(kms), ctypes.byref(kn), ctypes.byref(kfl)))
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([ms_total], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / a.steps
+    value = world * a.points * nmodes / (ms_step / 1e3)
+
+    bf16, hbm, src = peaks()
+    if a.form == "split":
+        peak = bf16 / 3.0
+        peak_note = "bf16_tflops burst / 3 (three FP16 hi/lo products per MAC), of %s" % src
+        bound = "tensor"
+        kernel = "k_split_l (tcgen05 kind::f16 contraction + operand generation)"
+    else:
+        peak = 1.25  # nominal FP64; no measured FP64 peak in MEASURED_PEAKS.json
+        peak_note = "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
+        bound = "fp64"
+        kernel = "k_fp64_raw_l"
+    achieved = (kfl.value / (kms.value / 1e3)) / 1e12 if kms.value > 0 else None
+    roof = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": None, "peak_source": peak_note,
+            "kernel_ms_per_step": kms.value / a.steps, "kernel_launches_per_step": int(kn.value) // max(1, a.steps),
+            "kernel_share_of_step": (kms.value / ms_total) if ms_total > 0 else None,
+            "algo_flops_per_point_mode": 4}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f16 hi+lo x3 / f32 accumulate / f64 reduce" if a.form == "split" else "f64",
+           "data": "synthetic", "config": workload_config(a), "gpu_launches": launches, "roofline": roof,
+           "clocks": clk}
+
+    if not a.no_extras and rank == 0:
+        # ---- e2e through the host-buffer C ABI (pinned input, H2D + compute + D2H) ----
+        kh = np.zeros(L * M)
+        ch = np.zeros(L * M)
+        times = []
+        for _ in range(max(1, min(a.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = _lib.lib.catana_gpu_sfb_raw(ctypes.c_void_p(h_pts.data_ptr()), ctypes.c_void_p(h_w.data_ptr()),
+                                             a.points, L, M, a.rmax, flags, _lib.ptr(kh), _lib.ptr(ch), None, sp)
+            _lib.check(st, "sfb_raw")
+            times.append(time.perf_counter() - t0)
+        e2e_t = float(np.median(times))
+        out["e2e"] = {"value": a.points * nmodes / e2e_t, "unit": UNIT, "ms_per_step": e2e_t * 1e3,
+                      "h2d_bytes_per_step": a.points * 32, "d2h_bytes_per_step": 2 * L * M * 8,
+                      "api": "catana_gpu_sfb_raw (host buffers, pinned)"}
+        # ---- FP64 plain GPU path on a subsample, and split-vs-plain accuracy ----
+        ns = min(a.plain_sample, a.points)
+        sub = np.ascontiguousarray(pts[:ns])
+        wsub = np.ascontiguousarray(w[:ns])
+        fc = int(_lib.lib.catana_gpu_flmn_size(L, M))
+        res = {}
+        for name, fl in (("plain", _lib.FORM_PLAIN | _lib.JL_EXACT), ("split", _lib.FORM_SPLIT)):
+            k2 = np.zeros(L * M)
+            c2 = np.zeros(L * M)
+            f2 = np.zeros(2 * fc)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _lib.check(_lib.lib.catana_gpu_sfb_raw(_lib.ptr(sub), _lib.ptr(wsub), ns, L, M, a.rmax, fl, _lib.ptr(k2),
+                                                   _lib.ptr(c2), _lib.ptr(f2), sp), name)
+            res[name] = (time.perf_counter() - t0, c2, f2)
+        tp = res["plain"][0]
+        cp_, fp_ = res["plain"][1], res["plain"][2]
+        cs_, fs_ = res["split"][1], res["split"][2]
+        fpz = fp_[0::2] + 1j * fp_[1::2]
+        fsz_ = fs_[0::2] + 1j * fs_[1::2]
+        out["plain_fp64"] = {"value": ns * nmodes / tp, "unit": UNIT, "sample_points": ns,
+                             "note": "FP64 CUDA-core path, exact j_l, host-buffer call incl. copies"}
+        if a.form == "split":
+            out["split_vs_plain_speedup"] = value / out["plain_fp64"]["value"]
+        rel = np.abs(cs_ - cp_) / np.abs(cp_)
+        cpm = cp_.reshape(L, M)
+        typ = np.abs(cs_ - cp_).reshape(L, M) / np.maximum(np.abs(cpm), np.median(cpm, axis=1, keepdims=True))
+        rms_l = []
+        off = 0
+        for l in range(L):
+            sl = slice(off, off + (l + 1) * M)
+            rms_l.append(np.sqrt(np.mean(np.abs(fsz_[sl] - fpz[sl]) ** 2) / np.mean(np.abs(fpz[sl]) ** 2)))
+            off += (l + 1) * M
+        out["accuracy_vs_fp64"] = {"sample_points": ns, "reference": "FP64 plain GPU path, exact j_l",
+                                   "c_ln_rel_err_median": float(np.median(rel)),
+                                   "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
+                                   "c_ln_rel_err_max": float(rel.max()),
+                                   "c_ln_abs_err_over_max_c_or_median_c_l_max": float(typ.max()),
+                                   "f_lmn_max_abs_err_over_max_f": float(np.max(np.abs(fsz_ - fpz)) /
+                                                                         np.max(np.abs(fpz))),
+                                   "f_lmn_rms_err_over_rms_f_by_l": {"l=0": float(rms_l[0]),
+                                                                     "l=%d" % (L // 2): float(rms_l[L // 2]),
+                                                                     "l=%d" % (L - 1): float(rms_l[-1])}}
+        # ---- CPU baseline: the oracle's OpenMP restatement on a bounded sample ----
+        cs = min(a.cpu_sample, a.points)
+        v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": "%d points (of %d), same lmax/nmax/rmax/weights, interpolated j_l as the "
+                                         "reference uses for N > 1000; %.1f s" % (cs, a.points, dt)}
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

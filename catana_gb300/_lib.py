@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libcatana_gpu.so")
 
 if not os.path.exists(LIB_PATH):
     raise ImportError(
-        "libcatana_gpu.so not found at %s; build it with `python -m catana_gb300.build` "
+        "libcatana_gpu.so not found at %s; build it with `python catana_gb300/build.py` "
         "(nvcc for sm_103a). catana_gb300 has no CPU fallback." % LIB_PATH)
 
 lib = ctypes.CDLL(LIB_PATH)
@@ -42,6 +42,8 @@ SIGNATURES = {
     "catana_gpu_sbessel_zeros": (ctypes.c_int, [_U32, _I32, _P]),
     "catana_gpu_compute_kln": (ctypes.c_int, [_U16, _U16, _D, _P]),
     "catana_gpu_last_error": (ctypes.c_char_p, []),
+    "catana_gpu_profile_enable": (None, [ctypes.c_int]),
+    "catana_gpu_profile_report": (ctypes.c_int, [_P, _P, _P]),
     "catana_gpu_launch_count": (ctypes.c_uint64, []),
 }
 

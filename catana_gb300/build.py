@@ -1,6 +1,7 @@
 """Build libcatana_gpu.so in-tree with nvcc for sm_103a.
 
-    python -m catana_gb300.build        (or catana_gb300.build.build())
+    python catana_gb300/build.py [-v]    (the package itself needs the built library,
+                                          so run this file directly)
 
 Each .cu under csrc/ is compiled to an object in parallel, then linked into
 catana_gb300/_lib/libcatana_gpu.so.  One -gencode (compute_103a -> sm_103a).
@@ -17,7 +18,9 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcatana_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction, so the Bessel-zero solve rounds the same on x86 and aarch64
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

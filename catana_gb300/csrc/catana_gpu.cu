@@ -26,6 +26,49 @@ static thread_local std::string t_last_error;
 void set_error(const std::string &msg) { t_last_error = msg; }
 
 // ---------------------------------------------------------------------------
+// Kernel timing
+// ---------------------------------------------------------------------------
+static std::atomic<int> g_prof_on{0};
+static std::mutex g_prof_mu;
+struct ProfRec {
+    cudaEvent_t a, b;
+    double flops;
+};
+static std::vector<ProfRec> g_prof;
+static std::vector<cudaEvent_t> g_prof_free;
+
+static cudaEvent_t prof_event() {
+    if (!g_prof_free.empty()) {
+        cudaEvent_t e = g_prof_free.back();
+        g_prof_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_begin(cudaStream_t st) {
+    if (!g_prof_on.load()) return;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    ProfRec r;
+    r.a = prof_event();
+    r.b = nullptr;
+    r.flops = 0.0;
+    cudaEventRecord(r.a, st);
+    g_prof.push_back(r);
+}
+
+void prof_end(cudaStream_t st, double algo_flops) {
+    if (!g_prof_on.load()) return;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    if (g_prof.empty() || g_prof.back().b) return;
+    g_prof.back().b = prof_event();
+    g_prof.back().flops = algo_flops;
+    cudaEventRecord(g_prof.back().b, st);
+}
+
+// ---------------------------------------------------------------------------
 // Bessel zeros: SphericalBesselZeros.cpp:11-68.  Asymptotic guesses for the first
 // two zeros (:17-47), Newton iterations that stop as soon as delta/z <= 1e-15 --
 // which includes every negative step (:49-62) -- and linear extrapolation
@@ -253,6 +296,36 @@ size_t catana_gpu_flmn_size(uint16_t lmax, uint16_t nmax) {
 const char *catana_gpu_last_error(void) { return t_last_error.c_str(); }
 
 uint64_t catana_gpu_launch_count(void) { return g_launches.load(); }
+
+void catana_gpu_profile_enable(int enable) { g_prof_on.store(enable ? 1 : 0); }
+
+catana_status_t catana_gpu_profile_report(double *kernel_ms, uint64_t *launches, double *algo_flops) {
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    double ms = 0.0, fl = 0.0;
+    uint64_t n = 0;
+    for (auto &r : g_prof) {
+        if (!r.b) continue;
+        cudaError_t e = cudaEventSynchronize(r.b);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
+            return CATANA_ERR_CUDA;
+        }
+        float t = 0.f;
+        cudaEventElapsedTime(&t, r.a, r.b);
+        ms += t;
+        fl += r.flops;
+        ++n;
+    }
+    for (auto &r : g_prof) {
+        g_prof_free.push_back(r.a);
+        if (r.b) g_prof_free.push_back(r.b);
+    }
+    g_prof.clear();
+    if (kernel_ms) *kernel_ms = ms;
+    if (launches) *launches = n;
+    if (algo_flops) *algo_flops = fl;
+    return CATANA_OK;
+}
 
 catana_status_t catana_gpu_sbessel_zeros(uint32_t l, int32_t count, double *out) {
     if (count < 0 || !out) {

@@ -18,6 +18,11 @@ inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_o
 
 void set_error(const std::string &msg);
 
+// Kernel timing (catana_gpu_profile_*): prof_begin/prof_end bracket one launch of
+// the dominant kernel when profiling is enabled.
+void prof_begin(cudaStream_t st);
+void prof_end(cudaStream_t st, double algo_flops);
+
 // Grow-only device buffer.
 struct DevBuf {
     void *ptr = nullptr;
@@ -40,6 +45,13 @@ struct DevBuf {
     }
 };
 
+// Cached split-form tables (per device): j_l piecewise polynomials, recurrence
+// coefficients and the largest |j_l| per l.
+struct SplitCache {
+    int lmax = -1, nmax = -1, nint = -1;
+    std::vector<double> maxj;
+};
+
 // Per-device state: workspace and cached tables.  Guarded by `mu`.
 struct DeviceContext {
     std::mutex mu;
@@ -58,6 +70,8 @@ struct DeviceContext {
     DevBuf io_points;  // staging of host inputs
     DevBuf io_out;     // staging of outputs
     DevBuf split_ws;   // split-form workspace
+    DevBuf split_tab;  // split-form tables
+    SplitCache split_cache;
     DevBuf hp_ws;      // HEALPix workspace
     // cache keys
     int coef_lmax = -1;
@@ -100,6 +114,10 @@ catana_status_t ensure_coefs(DeviceContext *ctx, int lmax, cudaStream_t st);
 catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
                                      int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
                                      double *f_acc_dev, int *err_dev, cudaStream_t st);
+
+// Stable radix sort of (key, index) pairs by the low key_bits bits (sort.cu).
+catana_status_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals, int64_t n,
+                                 int key_bits, uint32_t *hist_scratch, cudaStream_t st);
 
 // HEALPix (healpix.cu).
 catana_status_t healpix_bin_dev(DeviceContext *ctx, int64_t nside, const double *points_dev, int64_t npoints,

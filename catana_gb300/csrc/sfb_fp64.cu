@@ -373,6 +373,7 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
             a.partial = ctx->partial.as<double2>();
             a.err = err_dev;
             dim3 grid(nslabs, mb, nb);
+            prof_begin(st);
             if (big) {
                 const size_t sm = 3 * kTP * (64 + 1) * sizeof(double);
                 k_fp64_raw_l<64><<<grid, kThreads, sm, st>>>(a);
@@ -380,6 +381,7 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
                 const size_t sm = 3 * kTP * (32 + 1) * sizeof(double);
                 k_fp64_raw_l<32><<<grid, kThreads, sm, st>>>(a);
             }
+            prof_end(st, 4.0 * (double)nc * nmax * (l + 1));
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
             const int cnt = (l + 1) * nmax;

@@ -1,8 +1,803 @@
-// sfb_split.cu -- placeholder, replaced by the tcgen05 split-precision kernels.
+// sfb_split.cu -- split-precision raw SFB on the tcgen05 tensor cores (sm_103a).
+//
+// f_l(m, n) = k_ln * sum_i w_i j_l(k_ln r_i) P_lm(x_i) e^{-i m phi_i}  (sfb_raw.cpp:56-84)
+// computed per multipole l as the product D[n][col] = sum_i J[n][i] Y[i][col] with
+//   J[n][i] = w_i j_l(k_ln r_i) * 2^sJ          (A operand, 128 x K, FP16 hi + lo)
+//   Y[i][2m+0/1] = Re/Im P_lm(x_i) e^{-im phi_i} * 2^12   (B operand, K x 2 mcount)
+// and three tcgen05.mma kind::f16 products per K = 16 step (Jhi*Yhi + Jhi*Ylo +
+// Jlo*Yhi).  Both operands are scaled by powers of two towards the top of the FP16
+// range so the lo halves stay normal.
+//
+// Work split: one launch per l; a CTA owns one block of <= 128 complex m (so l >= 128
+// uses two CTAs per slab, each generating the J tile) and a slab of 32-point tiles.
+// Accumulation: the tensor core accumulates one tile (6 MMAs) into D_tile in tensor
+// memory; the CTA then folds D_tile into a second tensor-memory region D_acc with
+// FP32 round-to-nearest adds on the CUDA cores (the tensor core's own FP32
+// accumulation drifts measurably over long chains), and every FLUSH_FOLDS tiles adds
+// D_acc into the CTA's FP32 partial in global memory.  k_split_reduce sums the slab
+// partials in FP64 in fixed order and applies k_ln.
+//
+// Operand generation (CUDA cores, FP32 with float-float inputs):
+//   * j_l from a per-l piecewise degree-5 polynomial on intervals of width 1/2 in
+//     z = k r (Chebyshev interpolation of the FP64 j_l; error <= 1.2e-7 of the
+//     envelope including the FP32 coefficients), the argument formed as a float-float
+//     product so its absolute error is ~1e-12;
+//   * P_lm by one step of the l-recurrence from FP32 rows P_{l-1}, P_{l-2} in HBM
+//     (staged into shared memory one tile ahead with cp.async), with the recurrence
+//     coefficients and x = cos(theta), s = sin(theta) as float-float pairs; the rows
+//     are stored scaled by 2^100 so that sectoral seeds down to 2^-226 stay
+//     representable (enough for lmax <= 256);
+//   * e^{-i m phi}: one sincospif of the exact phase (64-bit fixed-point fraction of a
+//     turn) per warp-run of <= 8 m, then complex rotation by e^{i phi}.
+// Pipeline: two operand buffers and two row stages; the MMAs of tile t run while the
+// CTA generates tile t+1.  Every wait on an mbarrier is bounded (1 s); on timeout the
+// kernel records CATANA_ERR_CUDA in the error word, stops issuing work and frees its
+// tensor memory.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
 #include "common.cuh"
+#include "special.cuh"
+#include "tc05.cuh"
+
 namespace catana_gpu {
-catana_status_t split_raw_accumulate(DeviceContext *, const double *, const double *, int64_t, int, int, double,
-                                     const double *, double *, int *, cudaStream_t) {
-    return CATANA_ERR_UNSUPPORTED;
+
+namespace {
+
+constexpr int KT = 32;              // points per tile (two K=16 MMA steps)
+constexpr int NTHR = 512;           // 16 warps
+constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
+constexpr int FLUSH_FOLDS = 32;     // tiles folded into the TMEM sum before it goes to global memory
+constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
+constexpr double H = 0.5;           // table interval width in z
+constexpr int SPLIT_LMAX = 256;     // scaled-row range limit (see header comment)
+constexpr int SPLIT_NMAX = 128;     // one 128-lane accumulator tile
+constexpr uint64_t WAIT_NS = 1000000000ull;
+
+// shared-memory map (bytes, from a 1024-aligned base)
+constexpr uint32_t SM_J = 8192;          // J hi or J lo: 4 k-groups x 2 atoms
+constexpr uint32_t SM_Y = 16384;         // Y hi or Y lo: 4 k-groups x 4 atoms (256 columns)
+constexpr uint32_t SM_BUF = 2 * SM_J + 2 * SM_Y;
+constexpr uint32_t OFF_ST = 2 * SM_BUF;                // staged Legendre rows, two stages
+constexpr uint32_t SM_STROW = MBLK * KT * 4;           // one row set (MBLK m x 32 points) = 16 KB
+constexpr uint32_t SM_STPTS = KT * 48;                 // the tile's 32 SplitPt records
+constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS; // P_{l-1}, P_{l-2} and the points
+constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
+constexpr uint32_t SM_TAB = NINT_MAX * 32;
+constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;
+constexpr uint32_t OFF_COEF = OFF_KZ + SPLIT_NMAX * 8;
+constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
+
+constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
+// Y operand = P * 2^12: the stored rows carry 2^100, so the readout factor is 2^-88.
+// Scaling both operands towards the top of the FP16 range keeps the lo halves normal.
+constexpr float Y_UNSCALE = 3.2311742677852644e-27f;  // 2^-88
+constexpr float Y_SCALE = 4096.0f;                    // 2^12
+
+// Per-point operand inputs of the split form (48 bytes, radius-sorted order).
+struct SplitPt {
+    float r_hi, r_lo, w;        // radius (float-float), weight
+    float x_hi, x_lo;           // cos(theta) (float-float)
+    float s_hi, s_lo;           // sin(theta) (float-float)
+    float cphi, sphi, pad;      // e^{i phi}
+    unsigned long long u;       // phi / 2pi as a 64-bit fraction of a turn
+};
+static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
+
+struct SplitArgs {
+    int l, nmax, nint, nblocks;
+    int64_t n;          // points in the chunk
+    int stride;         // row stride of the Legendre rows (>= n, multiple of 32)
+    int tiles_per_cta;  // slab length in tiles
+    const SplitPt *pts;           // points of the chunk (sorted by radius)
+    const float *st1, *st2;       // scaled P_{l-1}^m, P_{l-2}^m rows [m][stride]
+    float *st0;                   // scaled P_l^m out
+    const float4 *coef;           // row l, m = 0..l
+    const float2 *kz;             // row l, n < nmax: k_ln / H as float-float
+    const float4 *tab;            // row l: nint intervals x 2 float4 (6 coefficients + pad)
+    float jscale;                 // 2^sJ
+    float inv_scale;              // 1 / (2^sJ * Y_SCALE)  (applied at flush)
+    float *partial;               // [slab][block][256][128]
+    int *err;
+};
+
+__device__ __forceinline__ void store_split8(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, const float (&v)[8]) {
+    uint32_t h[4], o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __half2 hh = __floats2half2_rn(v[2 * k], v[2 * k + 1]);
+        float2 hf = __half22float2(hh);
+        __half2 ll = __floats2half2_rn(v[2 * k] - hf.x, v[2 * k + 1] - hf.y);
+        h[k] = *reinterpret_cast<uint32_t *>(&hh);
+        o[k] = *reinterpret_cast<uint32_t *>(&ll);
+    }
+    *reinterpret_cast<uint4 *>(hi_base + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
 }
+
+// e^{i m phi} from the 64-bit phase fraction u = phi / 2pi:  (cos, sin)(2 pi frac(m u))
+__device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c, float &s) {
+    const unsigned long long t = (unsigned long long)m * u;  // mod 2^64: frac(m u) exactly
+    const int hi = (int)(t >> 32);                           // signed: frac in [-1/2, 1/2)
+    const float a = (float)hi * 4.656612873077393e-10f;      // 2^-31 -> value of 2 frac in [-1, 1)
+    sincospif(a, &s, &c);
+}
+
+// One CTA: multipole l, complex m in [128 b, 128 b + 128) of it (blockIdx.y = b),
+// a slab of 32-point tiles (blockIdx.x).
+__global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_base_sh;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int l = a.l;
+    const int mb0 = blockIdx.y * MBLK;
+    const int mcount = min(MBLK, l + 1 - mb0);
+    const int ncols = 2 * mcount;
+    const int ncols_pad = (ncols + 15) & ~15;
+    uint32_t half_cols = 32;
+    while ((int)half_cols < ncols_pad) half_cols <<= 1;
+    const uint32_t tcols = 2 * half_cols;  // D_tile at column 0, D_acc at column half_cols
+
+    float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
+    float2 *s_kz = reinterpret_cast<float2 *>(sm + OFF_KZ);
+    float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);
+    for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
+    for (int t = tid; t < a.nmax; t += NTHR) s_kz[t] = a.kz[t];
+    for (int t = tid; t < mcount; t += NTHR) s_coef[t] = a.coef[mb0 + t];
+    if (tid == 0) {
+        tc05::mbar_init(&mbar[0], 1);
+        tc05::mbar_init(&mbar[1], 1);
+    }
+    if (warp == 0) tc05::tmem_alloc(&tmem_base_sh, tcols);
+    tc05::fence_before();
+    __syncthreads();
+    tc05::fence_after();
+    const uint32_t tmem = tmem_base_sh;
+    const uint32_t d_tile = tmem, d_acc = tmem + half_cols;
+
+    const int64_t t0 = (int64_t)blockIdx.x * a.tiles_per_cta;
+    const int64_t ntiles_total = (a.n + KT - 1) / KT;
+    const int64_t t1 = min(ntiles_total, t0 + a.tiles_per_cta);
+    const int q = lane, g = warp;
+    const int MRW = (((mcount + 15) / 16) + 3) & ~3;  // m per warp, multiple of 4 (<= 8)
+    const int mlo = g * MRW, mhi = min(mlo + MRW, mcount);  // local m range of this warp
+    const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
+    const int stride = a.stride;
+    float *partial_cta = a.partial + ((size_t)blockIdx.x * a.nblocks + blockIdx.y) * 256 * 128;
+
+    uint32_t uses[2] = {0, 0}, waited[2] = {0, 0};
+    bool acc_fresh = true;   // next fold overwrites D_acc
+    bool first_flush = true; // partial rows not yet written by this CTA
+    int folds = 0;
+    bool ok = true;
+
+    auto wait_buf = [&](int b) -> bool {
+        while (waited[b] < uses[b]) {
+            if (!tc05::mbar_wait(&mbar[b], waited[b] & 1, WAIT_NS)) return false;
+            ++waited[b];
+        }
+        return true;
+    };
+
+    // stage the Legendre rows of tile t (this block's m) into stage buffer t&1
+    auto prefetch_rows = [&](int64_t t) {
+        if (t >= t1) return;
+        uint8_t *stg = sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE;
+        const int64_t i0 = t * KT;
+        // the tile's point records (the buffer is padded to whole tiles)
+        if (tid < (int)(SM_STPTS / 16))
+            tc05::cp_async16(stg + 2 * SM_STROW + tid * 16,
+                             reinterpret_cast<const uint8_t *>(a.pts + i0) + tid * 16);
+        if (l == 0) return;
+        const int per_set = mcount * 8;  // 16-byte pieces per row set
+        for (int c = tid; c < 2 * per_set; c += NTHR) {
+            const int which = c >= per_set;
+            const int rem = which ? c - per_set : c;
+            const int ml = rem >> 3, part = rem & 7;
+            const int m = mb0 + ml;
+            if (which && m > l - 2) continue;
+            const int msrc = (m == l) ? l - 1 : m;
+            const float *src = (which ? a.st2 : a.st1) + (int64_t)msrc * stride + i0 + part * 4;
+            tc05::cp_async16(stg + which * SM_STROW + ml * 128 + part * 16, src);
+        }
+    };
+
+    // D_acc (+)= D_tile, every warp: lane quadrant warp%4, column groups warp/4, +4, ...
+    auto fold = [&]() {
+        tc05::fence_after();
+        const int qd = warp & 3, cq = warp >> 2;
+        const uint32_t lane_off = (uint32_t)(qd * 32) << 16;
+        for (int gi = cq; gi < (ncols_pad >> 4); gi += 4) {
+            uint32_t vt[16], va[16];
+            tc05::tmem_ld16(d_tile + lane_off + gi * 16, vt);
+            if (!acc_fresh) tc05::tmem_ld16(d_acc + lane_off + gi * 16, va);
+            tc05::tmem_wait_ld();
+            if (!acc_fresh) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) vt[j] = __float_as_uint(__uint_as_float(vt[j]) + __uint_as_float(va[j]));
+            }
+            tc05::tmem_st16(d_acc + lane_off + gi * 16, vt);
+        }
+        tc05::tmem_wait_st();
+        acc_fresh = false;
+        ++folds;
+    };
+
+    // partial[cta] (+)= D_acc * inv_scale, then the next fold restarts D_acc
+    auto flush = [&]() {
+        tc05::fence_after();
+        const int qd = warp & 3, cq = warp >> 2;
+        const int lane_n = qd * 32 + lane;
+        for (int gi = cq; gi < (ncols_pad >> 4); gi += 4) {
+            uint32_t v[16];
+            tc05::tmem_ld16(d_acc + ((uint32_t)(qd * 32) << 16) + gi * 16, v);
+            tc05::tmem_wait_ld();
+            if (lane_n < a.nmax) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = gi * 16 + j;
+                    if (col < ncols) {
+                        const float d = __uint_as_float(v[j]) * a.inv_scale;
+                        float *p = partial_cta + (size_t)col * 128 + lane_n;
+                        *p = first_flush ? d : (*p + d);
+                    }
+                }
+            }
+        }
+        first_flush = false;
+        acc_fresh = true;
+        folds = 0;
+    };
+
+    prefetch_rows(t0);
+    tc05::cp_async_commit();
+    for (int64_t t = t0; t < t1 && ok; ++t) {
+        const int b = (int)((t - t0) & 1);
+        prefetch_rows(t + 1);
+        tc05::cp_async_commit();
+        // operand buffer b is free once the MMAs of tile t-2 have completed
+        const int w_ok = wait_buf(b) ? 1 : 0;
+        tc05::cp_async_wait_prev();
+        if (!__syncthreads_and(w_ok)) {
+            ok = false;
+            break;
+        }
+        uint8_t *bufp = sm + b * SM_BUF;
+        uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
+        const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
+        const float *stg2 = stg1 + MBLK * KT;
+        const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                                                                2 * SM_STROW + q * 48);
+        const int64_t i = t * KT + q;
+        const bool valid = i < a.n;
+        // ---- J tile: n = 8 g .. 8 g + 7 ----
+        {
+            float rh = 0.f, rl = 0.f, wj = 0.f;
+            if (valid) {
+                rh = pt.r_hi;
+                rl = pt.r_lo;
+                wj = pt.w * a.jscale;
+            }
+            const int n0 = 8 * g;
+            float v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int n = n0 + k;
+                float val = 0.f;
+                if (valid && n < a.nmax) {
+                    const float2 kk = s_kz[n];
+                    const float p = rh * kk.x;
+                    float e = fmaf(rh, kk.x, -p);
+                    e = fmaf(rh, kk.y, e);
+                    e = fmaf(rl, kk.x, e);
+                    const float fl = floorf(p);
+                    int idx = (int)fl;
+                    const float uu = (p - fl) + e;
+                    if ((unsigned)idx >= (unsigned)a.nint) {
+                        *a.err = CATANA_ERR_DOMAIN;
+                        idx = idx < 0 ? 0 : a.nint - 1;
+                    }
+                    const float4 c0 = s_tab[2 * idx], c1 = s_tab[2 * idx + 1];
+                    float jv = fmaf(c1.y, uu, c1.x);
+                    jv = fmaf(jv, uu, c0.w);
+                    jv = fmaf(jv, uu, c0.z);
+                    jv = fmaf(jv, uu, c0.y);
+                    jv = fmaf(jv, uu, c0.x);
+                    val = jv * wj;
+                }
+                v[k] = val;
+            }
+            store_split8(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v);
+        }
+        // ---- Y tile: local m = mlo .. mhi-1 of this block (groups of 4 complex = 8 columns) ----
+        if (mlo < mhi) {
+            float xh = 0.f, xl = 0.f, sh = 0.f, sl = 0.f, c1 = 1.f, s1 = 0.f;
+            unsigned long long uph = 0ull;
+            if (valid) {
+                xh = pt.x_hi;
+                xl = pt.x_lo;
+                sh = pt.s_hi;
+                sl = pt.s_lo;
+                c1 = pt.cphi;
+                s1 = pt.sphi;
+                uph = pt.u;
+            }
+            float cm, smv;
+            phase_seed(uph, mb0 + mlo, cm, smv);
+#pragma unroll
+            for (int gq = 0; gq < 2; ++gq) {
+                const int ml0 = mlo + 4 * gq;
+                if (ml0 < mhi) {
+                    float v[8];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int ml = ml0 + k;
+                        const int m = mb0 + ml;
+                        float yr = 0.f, yi = 0.f;
+                        if (ml < mhi && valid) {
+                            float P;
+                            if (l == 0) {
+                                P = P00_SCALED;
+                            } else {
+                                const float4 c = s_coef[ml];
+                                const float p1 = stg1[ml * KT + q];
+                                const bool sect = (m == l);
+                                const float xa = sect ? sh : xh, xb = sect ? sl : xl;
+                                const float tt = fmaf(xa, p1, xb * p1);
+                                const float p2 = (m <= l - 2) ? stg2[ml * KT + q] : 0.f;
+                                const float bb = fmaf(c.w, p2, c.z * p2);
+                                const float vv = fmaf(c.y, tt, -bb);
+                                P = fmaf(c.x, tt, vv);
+                            }
+                            a.st0[(int64_t)m * stride + i] = P;
+                            const float Pu = P * Y_UNSCALE;
+                            yr = Pu * cm;
+                            yi = -Pu * smv;
+                        }
+                        v[2 * k] = yr;
+                        v[2 * k + 1] = yi;
+                        // rotate e^{i m phi} -> e^{i (m+1) phi}
+                        const float nc = fmaf(cm, c1, -smv * s1);
+                        const float ns = fmaf(smv, c1, cm * s1);
+                        cm = nc;
+                        smv = ns;
+                    }
+                    store_split8(yhi, ylo, tc05::mn_sw128_off(2 * ml0, q, 4), v);
+                }
+            }
+        }
+        tc05::fence_proxy_async();
+        // ---- fold the previous tile's product into D_acc (needs its MMAs complete) ----
+        if (t > t0) {
+            const int pb = b ^ 1;
+            const int f_ok = wait_buf(pb) ? 1 : 0;
+            if (!__syncthreads_and(f_ok)) {
+                ok = false;
+                break;
+            }
+            fold();
+            if (folds == FLUSH_FOLDS) flush();
+        }
+        tc05::fence_before();
+        __syncthreads();
+        tc05::fence_after();
+        // ---- hand tile t to the tensor cores: D_tile = Jhi Yhi + Jhi Ylo + Jlo Yhi ----
+        if (tid == 0) {
+            const uint32_t sj_hi = tc05::smem_u32(jhi), sj_lo = tc05::smem_u32(jlo);
+            const uint32_t sy_hi = tc05::smem_u32(yhi), sy_lo = tc05::smem_u32(ylo);
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+                const uint64_t ah = tc05::desc_sw128(sj_hi + ks * 4096, 1024, 2048);
+                const uint64_t al = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
+                const uint64_t bh = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
+                const uint64_t bl = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
+                tc05::mma_f16(d_tile, ah, bh, idesc, ks == 0 ? 0u : 1u);
+                tc05::mma_f16(d_tile, ah, bl, idesc, 1u);
+                tc05::mma_f16(d_tile, al, bh, idesc, 1u);
+            }
+            tc05::commit(&mbar[b]);
+        }
+        ++uses[b];
+    }
+    // last tile: fold and flush
+    if (ok && t1 > t0) {
+        const int lb = (int)((t1 - 1 - t0) & 1);
+        ok = __syncthreads_and(wait_buf(lb) ? 1 : 0) != 0;
+        if (ok) {
+            fold();
+            flush();
+        }
+    }
+    if (ok) ok = __syncthreads_and((wait_buf(0) && wait_buf(1)) ? 1 : 0) != 0;
+    if (!ok) {
+        // give in-flight MMAs a last bounded chance to land before TMEM is released
+        wait_buf(0);
+        wait_buf(1);
+        if (tid == 0) *a.err = CATANA_ERR_CUDA;
+    }
+    tc05::cp_async_wait_all();
+    // an empty slab still owns partial rows: write zeros so the reduction sees them
+    if (t0 >= t1) {
+        for (int t = tid; t < ncols * 128; t += NTHR) partial_cta[t] = 0.f;
+    }
+    tc05::fence_before();
+    __syncthreads();
+    tc05::fence_after();
+    if (warp == 0) tc05::tmem_dealloc(tmem, tcols);
+}
+
+// f_acc[l][m][n] += k_ln[n] * sum_slab partial[slab][m / 128][2 (m % 128) + ri][n]  (FP64, slab order)
+__global__ void k_split_reduce(const float *__restrict__ partial, int nslabs, int nblocks, int lp1, int nmax,
+                               const double *__restrict__ kln_row, double2 *__restrict__ fl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (m, n)
+    if (t >= lp1 * nmax) return;
+    const int m = t / nmax, n = t - m * nmax;
+    const int blk = m / MBLK, ml = m - blk * MBLK;
+    double sr = 0.0, si = 0.0;
+    for (int s = 0; s < nslabs; ++s) {
+        const float *p = partial + ((size_t)s * nblocks + blk) * 256 * 128;
+        sr += (double)p[(size_t)(2 * ml) * 128 + n];
+        si += (double)p[(size_t)(2 * ml + 1) * 128 + n];
+    }
+    const double k = kln_row[n];
+    double2 o = fl[t];
+    o.x += k * sr;
+    o.y += k * si;
+    fl[t] = o;
+}
+
+// Point preparation, in radius-sorted order: float-float r, cos(theta), sin(theta);
+// e^{i phi} in FP32; the 64-bit phase fraction; FP32 weights.  Flags radii that are
+// negative or not finite.  Records past n (padding to whole tiles) are zeroed.
+__global__ void k_split_prep(const double *__restrict__ pts, const double *__restrict__ w,
+                             const uint32_t *__restrict__ perm, int64_t n, int64_t npad, SplitPt *out, int *err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    SplitPt o;
+    if (i >= n) {
+        o.r_hi = o.r_lo = o.w = o.x_hi = o.x_lo = o.s_hi = o.s_lo = o.cphi = o.sphi = o.pad = 0.f;
+        o.u = 0ull;
+        out[i] = o;
+        return;
+    }
+    const int64_t j = perm[i];
+    const double r = pts[3 * j], th = pts[3 * j + 1], ph = pts[3 * j + 2];
+    if (!(r >= 0.0) || !isfinite(r)) *err = CATANA_ERR_DOMAIN;
+    double st, ct, sp, cp;
+    sincos(th, &st, &ct);
+    sincos(ph, &sp, &cp);
+    o.r_hi = (float)r;
+    o.r_lo = (float)(r - (double)o.r_hi);
+    o.x_hi = (float)ct;
+    o.x_lo = (float)(ct - (double)o.x_hi);
+    o.s_hi = (float)st;
+    o.s_lo = (float)(st - (double)o.s_hi);
+    o.cphi = (float)cp;
+    o.sphi = (float)sp;
+    o.pad = 0.f;
+    double f = ph * 0.15915494309189533577;  // phi / 2pi
+    f -= floor(f);
+    const double scaled = ldexp(f, 64);
+    o.u = scaled >= 18446744073709551615.0 ? 0ull : (unsigned long long)scaled;
+    o.w = w ? (float)w[j] : 1.0f;
+    out[i] = o;
+}
+
+// radius keys for the sort: 16-bit quantisation of r / max_r, and the identity payload
+__global__ void k_split_keys(const double *__restrict__ pts, int64_t n, double inv_rmax, uint32_t *keys,
+                             uint32_t *vals) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double q = pts[3 * i] * inv_rmax * 65536.0;
+    keys[i] = q >= 65535.0 ? 65535u : (q > 0.0 ? (uint32_t)q : 0u);
+    vals[i] = (uint32_t)i;
+}
+
+// max(r) and max(|w|) as IEEE bit patterns of non-negative doubles
+__global__ void k_split_maxes(const double *__restrict__ pts, const double *__restrict__ w, int64_t n,
+                              unsigned long long *out) {
+    double mr = 0.0, mw = w ? 0.0 : 1.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double r = pts[3 * i];
+        if (r > mr) mr = r;
+        if (w) {
+            const double a = fabs(w[i]);
+            if (a > mw) mw = a;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(mr));
+        atomicMax(&out[1], (unsigned long long)__double_as_longlong(mw));
+    }
+}
+
+// j_l at the 6 Chebyshev nodes of every interval, all l at once per node (FP64).
+__global__ void k_split_nodes(int lmax, int nint, double *vals /* [node][lmax] */) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nint * 6) return;
+    const int j = node / 6, k = node - 6 * j;
+    const double tk = 0.5 - 0.5 * cos((2.0 * k + 1.0) * kPi / 12.0);  // Chebyshev node in [0, 1]
+    const double z = H * (j + tk);
+    double buf[SPLIT_LMAX + 1];
+    sbessel_jl_all(lmax, z, buf);
+    for (int l = 0; l < lmax; ++l) vals[(size_t)node * lmax + l] = buf[l];
+}
+
+// monomial coefficients in u in [0,1] of the interpolant through the 6 nodes
+__global__ void k_split_coefs(int lmax, int nint, const double *vals, const double *vinv /* 6x6 */,
+                              float4 *tab /* [l][nint][2] */) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lmax * nint) return;
+    const int l = t / nint, j = t - l * nint;
+    double y[6], c[6];
+    for (int k = 0; k < 6; ++k) y[k] = vals[(size_t)(6 * j + k) * lmax + l];
+    for (int r = 0; r < 6; ++r) {
+        double s = 0.0;
+        for (int k = 0; k < 6; ++k) s += vinv[6 * r + k] * y[k];
+        c[r] = s;
+    }
+    float4 *o = tab + ((size_t)l * nint + j) * 2;
+    o[0] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
+    o[1] = make_float4((float)c[4], (float)c[5], 0.f, 0.f);
+}
+
+void split_ff(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// inverse of the 6x6 Vandermonde matrix at the Chebyshev nodes (FP64, Gauss-Jordan)
+std::vector<double> cheb_vandermonde_inverse() {
+    double A[6][12];
+    for (int k = 0; k < 6; ++k) {
+        const double tk = 0.5 - 0.5 * std::cos((2.0 * k + 1.0) * kPi / 12.0);
+        double p = 1.0;
+        for (int r = 0; r < 6; ++r) {
+            A[k][r] = p;
+            p *= tk;
+        }
+        for (int r = 0; r < 6; ++r) A[k][6 + r] = (r == k) ? 1.0 : 0.0;
+    }
+    for (int col = 0; col < 6; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 6; ++r)
+            if (std::fabs(A[r][col]) > std::fabs(A[piv][col])) piv = r;
+        for (int c = 0; c < 12; ++c) std::swap(A[col][c], A[piv][c]);
+        const double d = A[col][col];
+        for (int c = 0; c < 12; ++c) A[col][c] /= d;
+        for (int r = 0; r < 6; ++r)
+            if (r != col) {
+                const double f = A[r][col];
+                for (int c = 0; c < 12; ++c) A[r][c] -= f * A[col][c];
+            }
+    }
+    // A[:, 6:] = V^{-1} with V[k][r] = t_k^r, so c = V^{-1} y
+    std::vector<double> inv(36);
+    for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < 6; ++k) inv[6 * r + k] = A[r][6 + k];
+    return inv;
+}
+
+}  // namespace
+
+catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
+                                     int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
+                                     double *f_acc_dev, int *err_dev, cudaStream_t st) {
+    if (lmax > SPLIT_LMAX || nmax > SPLIT_NMAX) {
+        set_error("the split form supports lmax <= 256 and nmax <= 128");
+        return CATANA_ERR_ARG;
+    }
+    if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
+    static bool attr = false;
+    if (!attr) {
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+        attr = true;
+    }
+    // ---- catalog extent: max r, max |w| ----
+    CG_CUDA_TRY(ctx->misc.ensure(256));
+    unsigned long long *mx = reinterpret_cast<unsigned long long *>(ctx->misc.as<char>() + 128);
+    CG_CUDA_TRY(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
+    k_split_maxes<<<std::min<int64_t>(4 * ctx->sm_count, ceil_div(npoints, 256)), 256, 0, st>>>(points_dev, weights_dev,
+                                                                                           npoints, mx);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    unsigned long long mxh[2];
+    CG_CUDA_TRY(cudaMemcpyAsync(mxh, mx, sizeof(mxh), cudaMemcpyDeviceToHost, st));
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    double max_r, max_w;
+    memcpy(&max_r, &mxh[0], 8);
+    memcpy(&max_w, &mxh[1], 8);
+    if (!(max_w > 0.0)) max_w = 1.0;
+    // ---- k_ln (host copy), table extent ----
+    std::vector<double> kh((size_t)lmax * nmax);
+    kln_table(lmax, nmax, rmax, kh.data());
+    double zmax = 0.0;
+    for (int l = 0; l < lmax; ++l) zmax = std::max(zmax, kh[(size_t)l * nmax + nmax - 1] * max_r);
+    const int nint = (int)std::ceil(zmax / H) + 1;
+    if (nint > NINT_MAX) {
+        set_error("split form: k_ln * max(r) exceeds the resident j_l table (max r beyond rmax?)");
+        return CATANA_ERR_DOMAIN;
+    }
+    // ---- tables (cached per lmax, nmax, nint) ----
+    SplitCache &C = ctx->split_cache;
+    const size_t tab_bytes = (size_t)lmax * nint * 2 * sizeof(float4);
+    const size_t coef_bytes = (size_t)lmax * (lmax + 1) / 2 * sizeof(float4);
+    const size_t kz_bytes = (size_t)lmax * nmax * sizeof(float2);
+    if (C.lmax != lmax || C.nmax != nmax || C.nint != nint) {
+        CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + coef_bytes + kz_bytes + 1024));
+        // node values (temporary, in the partial buffer's allocation)
+        const size_t vbytes = (size_t)nint * 6 * lmax * sizeof(double);
+        CG_CUDA_TRY(ctx->partial.ensure(vbytes + 36 * sizeof(double)));
+        double *vals = ctx->partial.as<double>();
+        double *vinv = vals + (size_t)nint * 6 * lmax;
+        std::vector<double> vi = cheb_vandermonde_inverse();
+        CG_CUDA_TRY(cudaMemcpyAsync(vinv, vi.data(), 36 * sizeof(double), cudaMemcpyHostToDevice, st));
+        k_split_nodes<<<ceil_div(nint * 6, 64), 64, 0, st>>>(lmax, nint, vals);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        float4 *tab = ctx->split_tab.as<float4>();
+        k_split_coefs<<<ceil_div((int64_t)lmax * nint, 128), 128, 0, st>>>(lmax, nint, vals, vinv, tab);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        // recurrence coefficients (A = a_lm, B = a_lm b_lm; sectoral and m = l-1 specials)
+        std::vector<float4> co((size_t)lmax * (lmax + 1) / 2);
+        for (int l = 0; l < lmax; ++l)
+            for (int m = 0; m <= l; ++m) {
+                double A = 0.0, B = 0.0;
+                if (l >= 1 && m == l) {
+                    A = -std::sqrt((2.0 * l + 1.0) / (2.0 * l));
+                } else if (l >= 1 && m == l - 1) {
+                    A = std::sqrt(2.0 * l + 1.0);
+                } else if (l >= 2) {
+                    const double dl = l, dl1 = l - 1, mm = (double)m * m;
+                    const double aa = std::sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+                    const double bb = std::sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
+                    A = aa;
+                    B = aa * bb;
+                }
+                float ah, al, bh, bl;
+                split_ff(A, ah, al);
+                split_ff(B, bh, bl);
+                co[(size_t)l * (l + 1) / 2 + m] = make_float4(ah, al, bh, bl);
+            }
+        float4 *coef_d = reinterpret_cast<float4 *>(reinterpret_cast<char *>(tab) + tab_bytes);
+        CG_CUDA_TRY(cudaMemcpyAsync(coef_d, co.data(), coef_bytes, cudaMemcpyHostToDevice, st));
+        C.maxj.assign(lmax, 1.0);
+        for (int l = 0; l < lmax; ++l) {
+            // largest |j_l| on [0, zmax]: sample around the first maximum (z ~ l + 0.8 l^(1/3))
+            double mj = (l == 0) ? 1.0 : 0.0;
+            if (l > 0) {
+                const double zc = l + 0.8 * std::cbrt((double)l);
+                for (int s = -200; s <= 400; ++s) {
+                    const double z = zc + 0.02 * s;
+                    if (z > 0) mj = std::max(mj, std::fabs(sbessel_jl(l, z)));
+                }
+                mj *= 1.05;
+            }
+            C.maxj[l] = mj;
+        }
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
+        C.lmax = lmax;
+        C.nmax = nmax;
+        C.nint = nint;
+    }
+    // per call: k as float-float, scaled by 1/H (depends on rmax)
+    float4 *tab = ctx->split_tab.as<float4>();
+    float4 *coef_d = reinterpret_cast<float4 *>(reinterpret_cast<char *>(tab) + tab_bytes);
+    float2 *kz_d = reinterpret_cast<float2 *>(reinterpret_cast<char *>(coef_d) + coef_bytes);
+    {
+        std::vector<float2> kz((size_t)lmax * nmax);
+        for (size_t t = 0; t < kz.size(); ++t) {
+            float hi, lo;
+            split_ff(kh[t] / H, hi, lo);
+            kz[t] = make_float2(hi, lo);
+        }
+        CG_CUDA_TRY(cudaMemcpyAsync(kz_d, kz.data(), kz_bytes, cudaMemcpyHostToDevice, st));
+    }
+    // J scale per l: a power of two that brings max |w j_l| into [2^14, 2^15): the
+    // typical |J| (j_l ~ 1/z at large z) then keeps a normal FP16 lo half.
+    std::vector<float> jscale(lmax);
+    for (int l = 0; l < lmax; ++l) {
+        const int e = (int)std::floor(std::log2(32768.0 / (C.maxj[l] * max_w)));
+        jscale[l] = (float)std::ldexp(1.0, std::max(-60, std::min(100, e)));
+    }
+
+    // ---- point chunks: sorted point records and three Legendre row sets ----
+    const int64_t chunk = std::max<int64_t>(KT, std::min<int64_t>(npoints, (int64_t)(16e9 / (12.0 * lmax))));
+    const int64_t stride = (chunk + 31) / 32 * 32;
+    auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t ptbytes = al256((size_t)stride * sizeof(SplitPt));
+    const size_t keybytes = al256((size_t)stride * sizeof(uint32_t));
+    const size_t histbytes = al256((size_t)256 * ((stride + 4095) / 4096) * sizeof(uint32_t));
+    const size_t rowbytes = al256((size_t)stride * lmax * sizeof(float));
+    CG_CUDA_TRY(ctx->split_ws.ensure(ptbytes + 4 * keybytes + histbytes + 3 * rowbytes));
+    char *ws = ctx->split_ws.as<char>();
+    SplitPt *spts = reinterpret_cast<SplitPt *>(ws);
+    uint32_t *keys = reinterpret_cast<uint32_t *>(ws + ptbytes);
+    uint32_t *perm = reinterpret_cast<uint32_t *>(ws + ptbytes + keybytes);
+    uint32_t *tkeys = reinterpret_cast<uint32_t *>(ws + ptbytes + 2 * keybytes);
+    uint32_t *tvals = reinterpret_cast<uint32_t *>(ws + ptbytes + 3 * keybytes);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(ws + ptbytes + 4 * keybytes);
+    float *rows[3];
+    for (int k = 0; k < 3; ++k)
+        rows[k] = reinterpret_cast<float *>(ws + ptbytes + 4 * keybytes + histbytes + k * rowbytes);
+
+    const int nblocks_max = (lmax + MBLK - 1) / MBLK;
+    const int slabs_max = std::max(1, ctx->sm_count);
+    CG_CUDA_TRY(ctx->partial.ensure((size_t)slabs_max * nblocks_max * 256 * 128 * sizeof(float)));
+    float *partial = ctx->partial.as<float>();
+
+    for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
+        const int64_t nc = std::min(chunk, npoints - c0);
+        const int64_t npad = (nc + KT - 1) / KT * KT;
+        k_split_keys<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, nc, max_r > 0.0 ? 1.0 / max_r : 0.0,
+                                                        keys, perm);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        catana_status_t ss = radix_sort_pairs(keys, perm, tkeys, tvals, nc, 16, hist, st);
+        if (ss != CATANA_OK) return ss;
+        k_split_prep<<<ceil_div(npad, 256), 256, 0, st>>>(points_dev + 3 * c0,
+                                                          weights_dev ? weights_dev + c0 : nullptr, perm, nc, npad,
+                                                          spts, err_dev);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        const int64_t ntiles = (nc + KT - 1) / KT;
+        float *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
+        for (int l = 0; l < lmax; ++l) {
+            const int nblocks = (l + 1 + MBLK - 1) / MBLK;
+            const int nslabs = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count / nblocks, ntiles));
+            const int tpc = (int)((ntiles + nslabs - 1) / nslabs);
+            SplitArgs a;
+            a.l = l;
+            a.nmax = nmax;
+            a.nint = nint;
+            a.nblocks = nblocks;
+            a.n = nc;
+            a.stride = (int)stride;
+            a.tiles_per_cta = tpc;
+            a.pts = spts;
+            a.st1 = st1;
+            a.st2 = st2;
+            a.st0 = st0;
+            a.coef = coef_d + (size_t)l * (l + 1) / 2;
+            a.kz = kz_d + (size_t)l * nmax;
+            a.tab = tab + (size_t)l * nint * 2;
+            a.jscale = jscale[l];
+            a.inv_scale = 1.0f / (jscale[l] * Y_SCALE);
+            a.partial = partial;
+            a.err = err_dev;
+            prof_begin(st);
+            k_split_l<<<dim3(nslabs, nblocks), NTHR, SMEM_BYTES, st>>>(a);
+            prof_end(st, 4.0 * (double)nc * nmax * (l + 1));
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            const int cnt = (l + 1) * nmax;
+            double2 *fl = reinterpret_cast<double2 *>(f_acc_dev) + (size_t)nmax * l * (l + 1) / 2;
+            k_split_reduce<<<ceil_div(cnt, 128), 128, 0, st>>>(partial, nslabs, nblocks, l + 1, nmax,
+                                                              kln_dev + (size_t)l * nmax, fl);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            float *t = st2;
+            st2 = st1;
+            st1 = st0;
+            st0 = t;
+        }
+    }
+    return CATANA_OK;
+}
+
 }  // namespace catana_gpu

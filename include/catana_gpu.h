@@ -133,6 +133,16 @@ catana_status_t catana_gpu_sbessel_zeros(uint32_t l, int32_t count, double *out)
 /* k_ln = z_{l,n} / rmax for l < lmax, n < nmax, row-major (return_types.cpp:10-20). */
 catana_status_t catana_gpu_compute_kln(uint16_t lmax, uint16_t nmax, double rmax, double *k_ln);
 
+/* Kernel timing for roofline reports.  While enabled, the library brackets every
+ * launch of the dominant contraction kernel (the tcgen05 split kernel or the FP64
+ * plain kernel) with CUDA events on the launching stream and records the launch's
+ * algorithmic work (4 flops per point-mode).  catana_gpu_profile_report()
+ * synchronises, returns the summed kernel time (ms), the number of timed launches
+ * and the summed algorithmic flops, and clears the record.  No counterpart in the
+ * reference (it has no GPU). */
+void catana_gpu_profile_enable(int enable);
+catana_status_t catana_gpu_profile_report(double *kernel_ms, uint64_t *launches, double *algo_flops);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char *catana_gpu_last_error(void);
 

@@ -211,6 +211,8 @@ void co_lerp_table(int l, double zmax, int npts, double *y, double *dx_inv_out)
 {
     double dx = (zmax - 0.0) / (npts - 1);
     *dx_inv_out = 1. / dx;
+    /* the reference fills its table in an OpenMP loop (FunctionInterpolator.cpp:15) */
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < npts; ++i) y[i] = co_sbessel_jl(l, 0.0 + (size_t)i * dx);
 }
 
