@@ -119,6 +119,9 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
 catana_status_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals, int64_t n,
                                  int key_bits, uint32_t *hist_scratch, cudaStream_t st);
 
+// In-place exclusive scan of uint32 words (sort.cu).
+catana_status_t scan_u32(uint32_t *data, int64_t count, cudaStream_t st);
+
 // HEALPix (healpix.cu).
 catana_status_t healpix_bin_dev(DeviceContext *ctx, int64_t nside, const double *points_dev, int64_t npoints,
                                 int64_t *offsets_dev, double *r_sorted_dev, int *err_dev, cudaStream_t st);

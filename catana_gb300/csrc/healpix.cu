@@ -1,15 +1,567 @@
-// healpix.cu -- placeholder, replaced by the HEALPix kernels.
+// healpix.cu -- HEALPix RING binning and the pixelized SFB (FP64).
+//
+// Binning (PixelizedPointContainer.cpp:11-30): ang2pix per point (RING scheme, the
+// published algorithm of Gorski et al. 2005, ApJ 622:759, sec. 4, evaluated in the
+// same operation order as the CPU restatement with every product and sum rounded
+// separately -- no FMA contraction -- so both give the same pixel), then a stable
+// radix sort of (pixel, point index) and a histogram scan give CSR offsets; radii are
+// gathered in point order within each pixel, as the reference's push_back does.
+//
+// SFB (sfb_reverse_fft.cpp:43-209), per multipole l:
+//   k_hp_map    map[pix][n] = sum_{p in pix} j_l(k_ln r_p), points in order
+//   k_hp_ylm    Y_lm(ring) = P_lm(cos theta_ring) e^{-i m phi_0(ring)} (phi_0: the ring's
+//               first pixel centre, as the reference's RingInfo)
+//   k_hp_ring   per ring: the real DFT F[s] = sum_j map_j e^{-2 pi i j s / rpix} at the
+//               frequencies the m-extraction reads, s = rpix/2 - |rpix/2 - (m mod rpix)|;
+//               the reference never conjugates (sign = (m > 0) scales only ... the sign
+//               of the imaginary part, which is +1 for every m > 0), so for
+//               m mod rpix > rpix/2 it uses F[rpix - m mod rpix] itself; the
+//               CATANA_HEALPIX_CONJ_FIX flag conjugates it.  Times Y_lm(ring) -> per-ring
+//               partial sums [ring][m][n]
+//   k_hp_reduce sum over rings in ring order; C_ln = (2 sum_m |f|^2 - |f_0|^2)
+//               (norm k)^2 / (2l+1) and f stored as f k norm (sfb_reverse_fft.cpp:147-153)
+// The ring transform is a direct DFT of only the needed frequencies, evaluated as a
+// small GEMM per ring (map chunk and twiddles staged in shared memory).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "common.cuh"
+#include "special.cuh"
+
 namespace catana_gpu {
-catana_status_t healpix_bin_dev(DeviceContext *, int64_t, const double *, int64_t, int64_t *, double *, int *,
-                                cudaStream_t) { return CATANA_ERR_UNSUPPORTED; }
-catana_status_t healpix_ang2pix_dev(int64_t, const double *, const double *, int64_t, int64_t *, int *,
-                                    cudaStream_t) { return CATANA_ERR_UNSUPPORTED; }
-catana_status_t healpix_pix2ang_dev(int64_t, const int64_t *, int64_t, double *, double *, cudaStream_t) {
-    return CATANA_ERR_UNSUPPORTED;
+
+namespace {
+
+constexpr double kInvHalfPi = 0.63661977236758134308;  // 2/pi
+
+__device__ __forceinline__ double fmodulo_d(double v1, double v2) {
+    if (v1 >= 0) return (v1 < v2) ? v1 : fmod(v1, v2);
+    const double tmp = __dadd_rn(fmod(v1, v2), v2);
+    return (tmp == v2) ? 0. : tmp;
 }
-catana_status_t healpix_sfb_dev(DeviceContext *, int64_t, const int64_t *, const double *, int64_t, int, int, bool,
-                                bool, const double *, double, double *, double *, int *, cudaStream_t) {
-    return CATANA_ERR_UNSUPPORTED;
+
+// RING ang2pix, theta in [0, pi]; -1 outside.
+__device__ int64_t ang2pix_ring_dev(int64_t nside, double theta, double phi) {
+    if (!(theta >= 0.0 && theta <= kPi)) return -1;
+    const int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    const bool have_sth = (theta < 0.01) || (theta > 3.14159 - 0.01);
+    const double z = cos(theta), sth = have_sth ? sin(theta) : 0.0;
+    const double za = fabs(z);
+    const double tt = fmodulo_d(__dmul_rn(phi, kInvHalfPi), 4.0);
+    const double dn = (double)nside;
+    if (za <= 2. / 3.) {
+        const int64_t nl4 = 4 * nside;
+        const double temp1 = __dmul_rn(dn, __dadd_rn(0.5, tt));
+        const double temp2 = __dmul_rn(__dmul_rn(dn, z), 0.75);
+        const int64_t jp = (int64_t)__dsub_rn(temp1, temp2);
+        const int64_t jm = (int64_t)__dadd_rn(temp1, temp2);
+        const int64_t ir = nside + 1 + jp - jm;
+        const int64_t kshift = 1 - (ir & 1);
+        const int64_t t1 = jp + jm - nside + kshift + 1 + nl4 + nl4;
+        const int64_t ip = (t1 >> 1) & (nl4 - 1);
+        return ncap + (ir - 1) * nl4 + ip;
+    }
+    const double tp = __dsub_rn(tt, (double)(int64_t)tt);
+    const double tmp = ((za < 0.99) || !have_sth)
+                           ? __dmul_rn(dn, sqrt(__dmul_rn(3.0, __dsub_rn(1.0, za))))
+                           : __ddiv_rn(__dmul_rn(dn, sth), sqrt(__ddiv_rn(__dadd_rn(1., za), 3.)));
+    const int64_t jp = (int64_t)__dmul_rn(tp, tmp);
+    const int64_t jm = (int64_t)__dmul_rn(__dsub_rn(1.0, tp), tmp);
+    const int64_t ir = jp + jm + 1;
+    int64_t ip = (int64_t)__dmul_rn(tt, (double)ir);
+    if (ip >= 4 * ir) ip -= 4 * ir;
+    return (z > 0) ? 2 * ir * (ir - 1) + ip : npix - 2 * ir * (ir + 1) + ip;
 }
+
+__device__ int64_t isqrt_dev(int64_t v) {
+    int64_t r = (int64_t)sqrt((double)v + 0.5);
+    while (r * r > v) --r;
+    while ((r + 1) * (r + 1) <= v) ++r;
+    return r;
+}
+
+__device__ void pix2ang_ring_dev(int64_t nside, int64_t pix, double *theta, double *phi) {
+    const int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    const double fact2 = __ddiv_rn(4., (double)npix), fact1 = __dmul_rn((double)(nside << 1), fact2);
+    double z, ph, sth = 0.0;
+    bool have_sth = false;
+    if (pix < ncap) {
+        const int64_t iring = (1 + isqrt_dev(1 + 2 * pix)) >> 1;
+        const int64_t iphi = (pix + 1) - 2 * iring * (iring - 1);
+        const double tmp = __dmul_rn((double)(iring * iring), fact2);
+        z = __dsub_rn(1.0, tmp);
+        if (z > 0.99) {
+            sth = sqrt(__dmul_rn(tmp, __dsub_rn(2.0, tmp)));
+            have_sth = true;
+        }
+        ph = __ddiv_rn(__dmul_rn(__dsub_rn((double)iphi, 0.5), 0.5 * kPi), (double)iring);
+    } else if (pix < (npix - ncap)) {
+        const int64_t nl4 = 4 * nside, ip = pix - ncap;
+        const int64_t tmp = ip / nl4;
+        const int64_t iring = tmp + nside, iphi = ip - nl4 * tmp + 1;
+        const double fodd = ((iring + nside) & 1) ? 1 : 0.5;
+        z = __dmul_rn((double)(2 * nside - iring), fact1);
+        ph = __dmul_rn(__dmul_rn(__dmul_rn(__dsub_rn((double)iphi, fodd), kPi), 0.75), fact1);
+    } else {
+        const int64_t ip = npix - pix;
+        const int64_t iring = (1 + isqrt_dev(2 * ip - 1)) >> 1;
+        const int64_t iphi = 4 * iring + 1 - (ip - 2 * iring * (iring - 1));
+        const double tmp = __dmul_rn((double)(iring * iring), fact2);
+        z = __dsub_rn(tmp, 1.0);
+        if (z < -0.99) {
+            sth = sqrt(__dmul_rn(tmp, __dsub_rn(2.0, tmp)));
+            have_sth = true;
+        }
+        ph = __ddiv_rn(__dmul_rn(__dsub_rn((double)iphi, 0.5), 0.5 * kPi), (double)iring);
+    }
+    *theta = have_sth ? atan2(sth, z) : acos(z);
+    *phi = ph;
+}
+
+__global__ void k_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix, int *err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t p = ang2pix_ring_dev(nside, theta[i], phi[i]);
+    if (p < 0) *err = CATANA_ERR_ARG;
+    pix[i] = p < 0 ? 0 : p;
+}
+
+__global__ void k_pix2ang(int64_t nside, const int64_t *pix, int64_t n, double *theta, double *phi) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    pix2ang_ring_dev(nside, pix[i], &theta[i], &phi[i]);
+}
+
+// keys = RING pixel of each point, vals = point index; counts[pix] += 1
+__global__ void k_bin_keys(int64_t nside, const double *pts, int64_t n, uint32_t *keys, uint32_t *vals,
+                           uint32_t *counts, int *err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int64_t p = ang2pix_ring_dev(nside, pts[3 * i + 1], pts[3 * i + 2]);
+    if (p < 0) {
+        *err = CATANA_ERR_ARG;
+        p = 0;
+    }
+    keys[i] = (uint32_t)p;
+    vals[i] = (uint32_t)i;
+    atomicAdd(&counts[p], 1u);
+}
+
+__global__ void k_bin_gather(const double *pts, const uint32_t *perm, int64_t n, const uint32_t *offs32,
+                             int64_t npix, double *r_sorted, int64_t *offs) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) r_sorted[i] = pts[3 * (int64_t)perm[i]];
+    if (i <= npix) offs[i] = (i == npix) ? n : (int64_t)offs32[i];
+}
+
+// map[pix][n] = sum over the pixel's points (in order) of j_l(k_ln r)
+__global__ void k_hp_map(const int64_t *__restrict__ offs, const double *__restrict__ r, int64_t npix, int nmax,
+                         const double *__restrict__ kln, const double *__restrict__ tab, int npts_tab, double dx_inv,
+                         double zmax, int l, double *__restrict__ map, int *err) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= npix * nmax) return;
+    const int64_t pix = t / nmax;
+    const int n = (int)(t - pix * nmax);
+    const double k = kln[n];
+    double s = 0.0;
+    for (int64_t q = offs[pix]; q < offs[pix + 1]; ++q) {
+        const double z = k * r[q];
+        double j;
+        if (tab) {
+            if (!(z >= 0.0) || z >= zmax) {
+                *err = CATANA_ERR_DOMAIN;
+                j = 0.0;
+            } else {
+                const double ia = z * dx_inv;
+                int ii = (int)ia;
+                if (ii > npts_tab - 2) ii = npts_tab - 2;
+                j = tab[ii] + (tab[ii + 1] - tab[ii]) * (ia - ii);
+            }
+        } else {
+            j = sbessel_jl(l, z);
+        }
+        s += j;
+    }
+    map[t] = s;
+}
+
+// Y_lm(ring) = P_lm(x_ring) e^{-i m phi_0}, thread per (ring, m)
+__global__ void k_hp_ylm(const double *__restrict__ ring_x, const double *__restrict__ ring_phi, int nrings, int l,
+                         const double2 *__restrict__ coef /* all rows, triangular */, double2 *__restrict__ ylm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrings * (l + 1)) return;
+    const int r = t / (l + 1), m = t - r * (l + 1);
+    const double x = ring_x[r];
+    // sectoral seed P_m^m, then the l-recurrence up to l (same coefficients as the raw path)
+    const double somx2 = sqrt((1.0 - x) * (1.0 + x));
+    double pmm = 0.28209479177387814347403972578038630;  // 1/sqrt(4 pi)
+    for (int i = 1; i <= m; ++i) pmm *= coef[(size_t)i * (i + 1) / 2 + i].x * somx2;
+    double p = pmm;
+    if (l > m) {
+        double p2 = pmm, p1 = coef[(size_t)(m + 1) * (m + 2) / 2 + m].x * (x * pmm);
+        for (int ll = m + 2; ll <= l; ++ll) {
+            const double2 c = coef[(size_t)ll * (ll + 1) / 2 + m];
+            const double pn = c.x * (x * p1 - c.y * p2);
+            p2 = p1;
+            p1 = pn;
+        }
+        p = p1;
+    }
+    double sn, cs;
+    sincos((double)m * ring_phi[r], &sn, &cs);
+    ylm[t] = make_double2(p * cs, -p * sn);
+}
+
+constexpr int HP_NB = 32;     // n per CTA
+constexpr int HP_MS = 8;      // m slots (threads) per n
+constexpr int HP_MPT = 8;     // m per thread -> 64 m per CTA
+constexpr int HP_JC = 64;     // pixels per staged map chunk
+constexpr int HP_MAXPIX = 4096;  // twiddle table capacity (ring length, 4 nside <= 4096)
+
+// per ring: G(m, n) = F_ring[s(m)](n) with the reference's extraction, times Y_lm(ring)
+__global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restrict__ map, int nmax, int l,
+                                                         const int64_t *__restrict__ ring_start,
+                                                         const int *__restrict__ ring_pix,
+                                                         const double2 *__restrict__ tw_all,
+                                                         const int64_t *__restrict__ tw_off,
+                                                         const double2 *__restrict__ ylm, int conj_fix,
+                                                         double2 *__restrict__ partial /* [ring][m][n] */) {
+    extern __shared__ double hp_smem[];
+    double2 *s_tw = reinterpret_cast<double2 *>(hp_smem);          // [rpix]
+    double *s_map = hp_smem + 2 * HP_MAXPIX;                        // [HP_JC][HP_NB]
+    const int r = blockIdx.x;
+    const int n0 = blockIdx.y * HP_NB, m0 = blockIdx.z * (HP_MS * HP_MPT);
+    const int rpix = ring_pix[r];
+    const int64_t rs = ring_start[r];
+    const int tid = threadIdx.x, nl = tid % HP_NB, ms = tid / HP_NB;
+    const int n = n0 + nl;
+    for (int k = tid; k < rpix; k += blockDim.x) s_tw[k] = tw_all[tw_off[r] + k];
+    // accumulators k < kval hold valid m = m0 + ms + HP_MS k <= l
+    const int kval = (l - m0 - ms) < 0 ? 0 : min(HP_MPT, (l - m0 - ms) / HP_MS + 1);
+    int sidx[HP_MPT], cur[HP_MPT];
+    double gr[HP_MPT], gi[HP_MPT];
+#pragma unroll
+    for (int k = 0; k < HP_MPT; ++k) {
+        const int m = m0 + ms + HP_MS * k;
+        const int mm = m % rpix;
+        int s = rpix / 2 - mm;
+        s = rpix / 2 - (s < 0 ? -s : s);
+        sidx[k] = s;
+        cur[k] = 0;
+        gr[k] = gi[k] = 0.0;
+    }
+    for (int j0 = 0; j0 < rpix; j0 += HP_JC) {
+        const int jn = min(HP_JC, rpix - j0);
+        __syncthreads();
+        for (int e = tid; e < HP_JC * HP_NB; e += blockDim.x) {
+            const int jj = e / HP_NB, nn = e % HP_NB;
+            s_map[e] = (jj < jn && n0 + nn < nmax) ? map[(rs + j0 + jj) * nmax + n0 + nn] : 0.0;
+        }
+        __syncthreads();
+        for (int jj = 0; jj < jn; ++jj) {
+            const double v = s_map[jj * HP_NB + nl];
+#pragma unroll
+            for (int k = 0; k < HP_MPT; ++k) {
+                if (k < kval) {
+                    const double2 w = s_tw[cur[k]];
+                    gr[k] = fma(v, w.x, gr[k]);
+                    gi[k] = fma(v, w.y, gi[k]);
+                    const int c = cur[k] + sidx[k];
+                    cur[k] = c >= rpix ? c - rpix : c;
+                }
+            }
+        }
+    }
+    if (n >= nmax) return;
+#pragma unroll
+    for (int k = 0; k < HP_MPT; ++k) {
+        const int m = m0 + ms + HP_MS * k;
+        if (m > l) continue;
+        const int mm = m % rpix;
+        double fr = gr[k], fi = gi[k];
+        if (m == 0) fi = 0.0;                                // sign = 0 at m = 0
+        if (conj_fix && 2 * mm > rpix) fi = -fi;             // the alias is the conjugate
+        const double2 y = ylm[(size_t)r * (l + 1) + m];
+        partial[((size_t)r * (l + 1) + m) * nmax + n] = make_double2(fr * y.x - fi * y.y, fr * y.y + fi * y.x);
+    }
+}
+
+// f(m, n) = sum over rings (ring order), stored as f k norm (sfb_reverse_fft.cpp:152-153)
+__global__ void k_hp_reduce(const double2 *__restrict__ partial, int nrings, int l, int nmax,
+                            const double *__restrict__ kln, double norm, double2 *__restrict__ fl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (l + 1) * nmax) return;
+    const int m = t / nmax, n = t - m * nmax;
+    double sr = 0.0, si = 0.0;
+    for (int r = 0; r < nrings; ++r) {
+        const double2 v = partial[((size_t)r * (l + 1) + m) * nmax + n];
+        sr += v.x;
+        si += v.y;
+    }
+    const double k = kln[n];
+    fl[t] = make_double2(sr * k * norm, si * k * norm);
+}
+
+// C_ln = (2 sum_m |f|^2 - |f_0|^2) / (2l+1) of the stored f (sfb_reverse_fft.cpp:147-150)
+__global__ void k_hp_cln(const double2 *__restrict__ fl, int l, int nmax, double *__restrict__ c_row) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nmax) return;
+    double sq = 0.0, f0 = 0.0;
+    for (int m = 0; m <= l; ++m) {
+        const double2 v = fl[(size_t)m * nmax + n];
+        const double a2 = v.x * v.x + v.y * v.y;
+        sq += a2;
+        if (m == 0) f0 = a2;
+    }
+    c_row[n] = (2 * sq - f0) / (2 * l + 1);
+}
+
+struct RingTables {
+    int64_t nside = -1;
+    int nrings = 0;
+    DevBuf buf;
+    size_t off_start = 0, off_pix = 0, off_x = 0, off_phi = 0, off_tw = 0, off_twoff = 0;
+};
+RingTables g_rings;
+
+// host copies of the HEALPix ring geometry (same formulas as the device functions)
+double fmodulo_h(double v1, double v2) {
+    if (v1 >= 0) return (v1 < v2) ? v1 : std::fmod(v1, v2);
+    const double tmp = std::fmod(v1, v2) + v2;
+    return (tmp == v2) ? 0. : tmp;
+}
+
+int64_t isqrt_h(int64_t v) {
+    int64_t r = (int64_t)std::sqrt((double)v + 0.5);
+    while (r * r > v) --r;
+    while ((r + 1) * (r + 1) <= v) ++r;
+    return r;
+}
+
+void pix2ang_h(int64_t nside, int64_t pix, double *theta, double *phi) {
+    const int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    const double fact2 = 4. / npix, fact1 = (nside << 1) * fact2;
+    double z, ph, sth = 0.0;
+    bool have_sth = false;
+    if (pix < ncap) {
+        const int64_t iring = (1 + isqrt_h(1 + 2 * pix)) >> 1;
+        const int64_t iphi = (pix + 1) - 2 * iring * (iring - 1);
+        const double tmp = (iring * iring) * fact2;
+        z = 1.0 - tmp;
+        if (z > 0.99) {
+            sth = std::sqrt(tmp * (2.0 - tmp));
+            have_sth = true;
+        }
+        ph = (iphi - 0.5) * (0.5 * kPi) / iring;
+    } else if (pix < (npix - ncap)) {
+        const int64_t nl4 = 4 * nside, ip = pix - ncap;
+        const int64_t tmp = ip / nl4;
+        const int64_t iring = tmp + nside, iphi = ip - nl4 * tmp + 1;
+        const double fodd = ((iring + nside) & 1) ? 1 : 0.5;
+        z = (2 * nside - iring) * fact1;
+        ph = (iphi - fodd) * kPi * 0.75 * fact1;
+    } else {
+        const int64_t ip = npix - pix;
+        const int64_t iring = (1 + isqrt_h(2 * ip - 1)) >> 1;
+        const int64_t iphi = 4 * iring + 1 - (ip - 2 * iring * (iring - 1));
+        const double tmp = (iring * iring) * fact2;
+        z = tmp - 1.0;
+        if (z < -0.99) {
+            sth = std::sqrt(tmp * (2.0 - tmp));
+            have_sth = true;
+        }
+        ph = (iphi - 0.5) * (0.5 * kPi) / iring;
+    }
+    *theta = have_sth ? std::atan2(sth, z) : std::acos(z);
+    *phi = ph;
+}
+
+catana_status_t ensure_rings(int64_t nside, cudaStream_t st) {
+    RingTables &R = g_rings;
+    if (R.nside == nside) return CATANA_OK;
+    const int nrings = (int)(4 * nside - 1);
+    const int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    std::vector<int64_t> start(nrings), twoff(nrings);
+    std::vector<int> rp(nrings);
+    std::vector<double> x(nrings), ph(nrings);
+    // twiddles, one table per ring length 4 i (i = 1 .. nside), offset 2 i (i - 1)
+    std::vector<double2> tw((size_t)2 * nside * (nside + 1));
+    for (int64_t i = 1; i <= nside; ++i) {
+        const int64_t len = 4 * i, off = 2 * i * (i - 1);
+        for (int64_t k = 0; k < len; ++k) {
+            const double a = -2.0 * kPi * (double)k / (double)len;
+            tw[off + k] = make_double2(std::cos(a), std::sin(a));
+        }
+    }
+    for (int r = 0; r < nrings; ++r) {  // get_ring_info_small(r + 1)
+        const int64_t ring = r + 1;
+        int64_t s, len;
+        if (ring < nside) {
+            len = 4 * ring;
+            s = 2 * ring * (ring - 1);
+        } else if (ring < 3 * nside) {
+            len = 4 * nside;
+            s = ncap + (ring - nside) * 4 * nside;
+        } else {
+            const int64_t nr = 4 * nside - ring;
+            len = 4 * nr;
+            s = npix - 2 * nr * (nr + 1);
+        }
+        start[r] = s;
+        rp[r] = (int)len;
+        const int64_t i = len / 4;
+        twoff[r] = 2 * i * (i - 1);
+        double th, phi;
+        pix2ang_h(nside, s, &th, &phi);
+        x[r] = std::cos(th);  // RingInfo: cos(theta) of the first pixel (sfb_reverse_fft.cpp:21)
+        ph[r] = phi;
+    }
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    R.off_start = 0;
+    R.off_pix = al(R.off_start + nrings * sizeof(int64_t));
+    R.off_x = al(R.off_pix + nrings * sizeof(int));
+    R.off_phi = al(R.off_x + nrings * sizeof(double));
+    R.off_twoff = al(R.off_phi + nrings * sizeof(double));
+    R.off_tw = al(R.off_twoff + nrings * sizeof(int64_t));
+    const size_t total = R.off_tw + tw.size() * sizeof(double2);
+    CG_CUDA_TRY(R.buf.ensure(total));
+    char *b = R.buf.as<char>();
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_start, start.data(), nrings * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_pix, rp.data(), nrings * sizeof(int), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_x, x.data(), nrings * sizeof(double), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_phi, ph.data(), nrings * sizeof(double), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_twoff, twoff.data(), nrings * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    R.nside = nside;
+    R.nrings = nrings;
+    return CATANA_OK;
+}
+
+}  // namespace
+
+catana_status_t healpix_ang2pix_dev(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,
+                                    int *err_dev, cudaStream_t st) {
+    if (n == 0) return CATANA_OK;
+    k_ang2pix<<<ceil_div(n, 256), 256, 0, st>>>(nside, theta, phi, n, pix, err_dev);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    return CATANA_OK;
+}
+
+catana_status_t healpix_pix2ang_dev(int64_t nside, const int64_t *pix, int64_t n, double *theta, double *phi,
+                                    cudaStream_t st) {
+    if (n == 0) return CATANA_OK;
+    k_pix2ang<<<ceil_div(n, 256), 256, 0, st>>>(nside, pix, n, theta, phi);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    return CATANA_OK;
+}
+
+catana_status_t healpix_bin_dev(DeviceContext *ctx, int64_t nside, const double *points_dev, int64_t npoints,
+                                int64_t *offsets_dev, double *r_sorted_dev, int *err_dev, cudaStream_t st) {
+    const int64_t npix = 12 * nside * nside;
+    if (npoints > (int64_t)0xFFFFFFFFll - 1) {
+        set_error("bin_points: at most 2^32 - 2 points");
+        return CATANA_ERR_ARG;
+    }
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t nb = al((size_t)std::max<int64_t>(npoints, 1) * sizeof(uint32_t));
+    const size_t cb = al((size_t)(npix + 1) * sizeof(uint32_t));
+    const size_t hb = al((size_t)256 * ((npoints + 4095) / 4096 + 1) * sizeof(uint32_t));
+    CG_CUDA_TRY(ctx->hp_ws.ensure(4 * nb + cb + hb));
+    char *w = ctx->hp_ws.as<char>();
+    uint32_t *keys = reinterpret_cast<uint32_t *>(w), *vals = reinterpret_cast<uint32_t *>(w + nb);
+    uint32_t *tk = reinterpret_cast<uint32_t *>(w + 2 * nb), *tv = reinterpret_cast<uint32_t *>(w + 3 * nb);
+    uint32_t *counts = reinterpret_cast<uint32_t *>(w + 4 * nb);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(w + 4 * nb + cb);
+    CG_CUDA_TRY(cudaMemsetAsync(counts, 0, (npix + 1) * sizeof(uint32_t), st));
+    if (npoints > 0) {
+        k_bin_keys<<<ceil_div(npoints, 256), 256, 0, st>>>(nside, points_dev, npoints, keys, vals, counts, err_dev);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        int bits = 0;
+        while ((int64_t(1) << bits) < npix) bits += 8;
+        catana_status_t s = radix_sort_pairs(keys, vals, tk, tv, npoints, bits, hist, st);
+        if (s != CATANA_OK) return s;
+    }
+    // exclusive scan of the counts -> pixel offsets (uint32), then widen to int64
+    catana_status_t s = scan_u32(counts, npix, st);
+    if (s != CATANA_OK) return s;
+    const int64_t nthreads = std::max<int64_t>(npoints, npix + 1);
+    k_bin_gather<<<ceil_div(nthreads, 256), 256, 0, st>>>(points_dev, vals, npoints, counts, npix, r_sorted_dev,
+                                                          offsets_dev);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    return CATANA_OK;
+}
+
+catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t *offsets_dev,
+                                const double *r_sorted_dev, int64_t npoints, int lmax, int nmax, bool interpolated,
+                                bool conj_fix, const double *kln_dev, double norm, double *f_dev, double *c_ln_dev,
+                                int *err_dev, cudaStream_t st) {
+    if (lmax == 0 || nmax == 0) return CATANA_OK;
+    if (4 * nside > HP_MAXPIX) {
+        set_error("HEALPix path supports nside <= 1024");
+        return CATANA_ERR_ARG;
+    }
+    catana_status_t s = ensure_coefs(ctx, lmax + 1, st);
+    if (s != CATANA_OK) return s;
+    if (interpolated) {
+        s = ensure_lerp_tables(ctx, lmax, nmax, st);
+        if (s != CATANA_OK) return s;
+    }
+    s = ensure_rings(nside, st);
+    if (s != CATANA_OK) return s;
+    RingTables &R = g_rings;
+    const int64_t npix = 12 * nside * nside;
+    const int nrings = R.nrings;
+    char *rb = R.buf.as<char>();
+    const int64_t *ring_start = reinterpret_cast<const int64_t *>(rb + R.off_start);
+    const int *ring_pix = reinterpret_cast<const int *>(rb + R.off_pix);
+    const double *ring_x = reinterpret_cast<const double *>(rb + R.off_x);
+    const double *ring_phi = reinterpret_cast<const double *>(rb + R.off_phi);
+    const int64_t *tw_off = reinterpret_cast<const int64_t *>(rb + R.off_twoff);
+    const double2 *tw = reinterpret_cast<const double2 *>(rb + R.off_tw);
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t mapb = al((size_t)npix * nmax * sizeof(double));
+    const size_t ylmb = al((size_t)nrings * lmax * sizeof(double2));
+    const size_t partb = al((size_t)nrings * lmax * nmax * sizeof(double2));
+    CG_CUDA_TRY(ctx->partial.ensure(mapb + ylmb + partb));
+    double *map = ctx->partial.as<double>();
+    double2 *ylm = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb);
+    double2 *partial = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb + ylmb);
+    const int npts_tab = 1000 * nmax;
+    const size_t smem = (2 * HP_MAXPIX + HP_JC * HP_NB) * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_hp_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    for (int l = 0; l < lmax; ++l) {
+        k_hp_map<<<ceil_div(npix * nmax, 256), 256, 0, st>>>(
+            offsets_dev, r_sorted_dev, npix, nmax, kln_dev + (size_t)l * nmax,
+            interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr, npts_tab,
+            interpolated ? ctx->tab_dxinv[l] : 0.0, interpolated ? ctx->tab_zmax[l] : 0.0, l, map, err_dev);
+        k_hp_ylm<<<ceil_div(nrings * (l + 1), 128), 128, 0, st>>>(ring_x, ring_phi, nrings, l, ctx->coef.as<double2>(),
+                                                                  ylm);
+        dim3 grid(nrings, ceil_div(nmax, HP_NB), ceil_div(l + 1, HP_MS * HP_MPT));
+        prof_begin(st);
+        k_hp_ring<<<grid, HP_NB * HP_MS, smem, st>>>(map, nmax, l, ring_start, ring_pix, tw, tw_off, ylm,
+                                                     conj_fix ? 1 : 0, partial);
+        prof_end(st, 4.0 * (double)npix * nmax * (l + 1));
+        double2 *fl = reinterpret_cast<double2 *>(f_dev) + (size_t)nmax * l * (l + 1) / 2;
+        k_hp_reduce<<<ceil_div((l + 1) * nmax, 128), 128, 0, st>>>(partial, nrings, l, nmax,
+                                                                   kln_dev + (size_t)l * nmax, norm, fl);
+        k_hp_cln<<<ceil_div(nmax, 64), 64, 0, st>>>(fl, l, nmax, c_ln_dev + (size_t)l * nmax);
+        count_launch(5);
+        CG_CUDA_TRY(cudaGetLastError());
+    }
+    return CATANA_OK;
+}
+
 }  // namespace catana_gpu

@@ -107,6 +107,16 @@ __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_
 
 }  // namespace
 
+// In-place exclusive scan of count uint32 words (single CTA; counts up to a few
+// million entries).
+catana_status_t scan_u32(uint32_t *data, int64_t count, cudaStream_t st) {
+    if (count <= 0) return CATANA_OK;
+    k_radix_scan<<<1, 1024, 0, st>>>(data, count);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    return CATANA_OK;
+}
+
 // Sorts (keys, vals) by the low `key_bits` bits of the keys, stably.  The result
 // ends in (keys, vals); tmp_keys / tmp_vals are scratch of n entries; hist_scratch
 // holds 256 * ceil(n / 4096) words.
