@@ -53,8 +53,9 @@ typedef enum {
 #define CATANA_JL_MASK 3u
 /* Contraction form.  PLAIN: FP64 on CUDA cores, the drop-in.  SPLIT: tensor-core
  * tcgen05 contraction of 3-term FP16 hi+lo products with FP32 accumulation,
- * FP64 across point chunks; j_l from a piecewise-cubic table accurate to ~1e-8
- * (the JL flags do not apply). */
+ * folded per 32-point tile and reduced in FP64; j_l from a piecewise degree-5 table
+ * accurate to ~1.2e-7 of its envelope (the JL flags do not apply); lmax <= 256,
+ * nmax <= 128. */
 #define CATANA_FORM_PLAIN 0u
 #define CATANA_FORM_SPLIT 4u
 #define CATANA_FORM_MASK 4u
