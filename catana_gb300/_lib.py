@@ -35,6 +35,7 @@ SIGNATURES = {
     "catana_gpu_flmn_size": (ctypes.c_size_t, [_U16, _U16]),
     "catana_gpu_sfb_raw": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_sfb_raw_dev": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P, _P]),
+    "catana_gpu_sfb_raw_noalloc": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_bin_points": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
     "catana_gpu_ang2pix_ring": (ctypes.c_int, [_I64, _P, _P, _I64, _P, _P]),

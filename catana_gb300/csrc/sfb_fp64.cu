@@ -24,6 +24,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -408,4 +410,238 @@ catana_status_t finish_flmn_cln(double *f_dev, double norm, int lmax, int nmax, 
     return CATANA_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point: catana_gpu_sfb_raw_noalloc.
+//
+// For callers that cannot allocate device memory themselves or let a library do
+// it (code running under a caller-owned memory pool or a fixed memory budget, or
+// work that must not trigger cudaMalloc's implicit device synchronisation), this
+// runs the plain FP64 raw path with all of its scratch -- point SoA, Legendre rows,
+// slab partial sums, recurrence coefficients, interpolation tables, the error and
+// weight-sum words -- carved out of one fixed static device array, kNoAllocBytes per
+// device, held for the life of the process.  The first call on each device resolves
+// the array's device address with cudaGetSymbolAddress (make that first call before
+// any stream capture).  Every call shares the array: overlapping calls on the GPU
+// (two host threads, or several streams) race on it.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+unsigned char *g_noalloc_base[kNoAllocMaxDevices] = {nullptr};
+constexpr int kNoAllocMaxSlabs = 256;
+
+__global__ void k_noalloc_wsum(const double *w, int64_t n, double *out) {
+    __shared__ double sh[1024];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += w[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+}  // namespace
+
+}  // namespace catana_gpu
+
+using namespace catana_gpu;
+
+extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, const double *weights_dev,
+                                                     int64_t npoints, uint16_t lmax, uint16_t nmax, double rmax,
+                                                     uint32_t flags, double *k_ln_dev, double *c_ln_dev,
+                                                     double *f_lmn_dev, catana_gpu_stream_t stream) {
+    if (npoints < 0 || !(rmax > 0.0) || !std::isfinite(rmax)) {
+        set_error("sfb_raw_noalloc: npoints must be >= 0 and rmax positive and finite");
+        return CATANA_ERR_ARG;
+    }
+    if ((flags & CATANA_FORM_MASK) != CATANA_FORM_PLAIN) {
+        set_error("sfb_raw_noalloc: only the plain FP64 form runs allocation-free");
+        return CATANA_ERR_ARG;
+    }
+    const size_t lm = (size_t)lmax * nmax;
+    if (lm && (!k_ln_dev || !c_ln_dev || !f_lmn_dev)) {
+        set_error("sfb_raw_noalloc: k_ln, c_ln and f_lmn device buffers are required");
+        return CATANA_ERR_ARG;
+    }
+    if (npoints > 0 && !points_dev) {
+        set_error("sfb_raw_noalloc: null points");
+        return CATANA_ERR_ARG;
+    }
+    const uint32_t jl = flags & CATANA_JL_MASK;
+    const bool interpolated = jl == CATANA_JL_INTERP || (jl == CATANA_JL_AUTO && npoints > 1000);
+    // scratch plan: [words 256 B][coefficients][tables + dx][SoA][3 Legendre rows][partials]
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const int L = std::max<int>(lmax, 2);
+    const int npts_tab = 1000 * nmax;
+    const size_t b_words = 256;
+    const size_t b_coef = al((size_t)L * (L + 1) * sizeof(double));
+    const size_t b_tab = interpolated ? al(((size_t)lmax * npts_tab + lmax) * sizeof(double)) : 0;
+    const size_t b_part = al((size_t)kNoAllocMaxSlabs * lmax * nmax * sizeof(double2));
+    const size_t fixed = b_words + b_coef + b_tab + b_part;
+    const size_t per_point = (4 + 3 * (size_t)std::max<int>(lmax, 1)) * sizeof(double);
+    const int64_t min_chunk = std::min<int64_t>(std::max<int64_t>(npoints, 1), 1024);
+    if (fixed + (size_t)min_chunk * per_point + 256 > kNoAllocBytes) {
+        set_error("sfb_raw_noalloc: lmax=" + std::to_string(lmax) + ", nmax=" + std::to_string(nmax) +
+                  " needs more than the " + std::to_string(kNoAllocBytes >> 20) +
+                  " MiB allocation-free scratch (the tables and partial sums grow with lmax * nmax)");
+        return CATANA_ERR_ARG;
+    }
+    int dev = 0;
+    CG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("sfb_raw_noalloc: device index out of range");
+        return CATANA_ERR_ARG;
+    }
+    int cs;
+    DeviceContext *ctx = get_context(&cs);  // device properties only; its buffers are not used
+    if (!ctx) return (catana_status_t)cs;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        void *p = nullptr;
+        CG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_base[dev] = static_cast<unsigned char *>(p);
+    }
+    unsigned char *base = g_noalloc_base[dev];
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int *err_d = reinterpret_cast<int *>(base);
+    double *wsum_d = reinterpret_cast<double *>(base + 64);
+    double2 *coef_d = reinterpret_cast<double2 *>(base + b_words);
+    double *tab_d = reinterpret_cast<double *>(base + b_words + b_coef);
+    double2 *part_d = reinterpret_cast<double2 *>(base + b_words + b_coef + b_tab);
+    unsigned char *var = base + fixed;
+    const size_t var_bytes = kNoAllocBytes - fixed;
+    int64_t chunk = (int64_t)(var_bytes / per_point);
+    chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(npoints, 1)));
+    double *soa = reinterpret_cast<double *>(var);
+    double *rows0 = soa + 4 * chunk;
+
+    CG_CUDA_TRY(cudaMemsetAsync(err_d, 0, sizeof(int), st));
+    // k_ln on the host (cached zeros of the reference's zero finder)
+    std::vector<double> kh(lm);
+    kln_table(lmax, nmax, rmax, kh.data());
+    if (lm) CG_CUDA_TRY(cudaMemcpyAsync(k_ln_dev, kh.data(), lm * sizeof(double), cudaMemcpyHostToDevice, st));
+    const size_t fbytes = catana_gpu_flmn_size(lmax, nmax) * 2 * sizeof(double);
+    if (fbytes) CG_CUDA_TRY(cudaMemsetAsync(f_lmn_dev, 0, fbytes, st));
+    if (lm == 0) return CATANA_OK;
+    // recurrence coefficients (same values as the cached table of the plain path)
+    std::vector<double> ch((size_t)L * (L + 1));
+    for (int l = 0; l < L; ++l) {
+        double *row = ch.data() + (size_t)l * (l + 1);
+        for (int m = 0; m <= l; ++m) {
+            double ca = 0.0, cb = 0.0;
+            if (l >= 1 && m == l) {
+                ca = -sqrt((2.0 * l + 1.0) / (2.0 * l));
+            } else if (l >= 1 && m == l - 1) {
+                ca = sqrt(2.0 * l + 1.0);
+            } else if (l >= 2) {
+                const double dl = l, dl1 = l - 1, mm = (double)m * m;
+                ca = sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+                cb = sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
+            }
+            row[2 * m] = ca;
+            row[2 * m + 1] = cb;
+        }
+    }
+    CG_CUDA_TRY(cudaMemcpyAsync(coef_d, ch.data(), ch.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    // interpolation tables, rebuilt each call (the array keeps whatever the last call left)
+    std::vector<double> dx(lmax), dxinv(lmax), zmx(lmax);
+    if (interpolated) {
+        for (int l = 0; l < lmax; ++l) {
+            zmx[l] = zeros_for((unsigned)l, nmax + 1)[nmax];
+            dx[l] = (zmx[l] - 0.0) / (npts_tab - 1);
+            dxinv[l] = 1. / dx[l];
+        }
+        double *dx_d = tab_d + (size_t)lmax * npts_tab;
+        CG_CUDA_TRY(cudaMemcpyAsync(dx_d, dx.data(), lmax * sizeof(double), cudaMemcpyHostToDevice, st));
+        const int64_t total = (int64_t)lmax * npts_tab;
+        k_lerp_tables<<<ceil_div(total, 256), 256, 0, st>>>(tab_d, dx_d, lmax, npts_tab);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+    }
+    CG_CUDA_TRY(cudaFuncSetAttribute(k_fp64_raw_l<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(3 * kTP * (64 + 1) * sizeof(double))));
+    double *rows[3];
+    for (int k = 0; k < 3; ++k) rows[k] = rows0 + (size_t)k * chunk * std::max<int>(lmax, 1);
+    for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
+        const int64_t nc = std::min(chunk, npoints - c0);
+        double *r = soa, *x = soa + chunk, *ph = soa + 2 * chunk, *w = soa + 3 * chunk;
+        k_prep_points<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, weights_dev ? weights_dev + c0 : nullptr,
+                                                         nc, r, x, ph, w);
+        count_launch();
+        double *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
+        for (int l = 0; l < lmax; ++l) {
+            const bool big = (l + 1 > 32) || (nmax > 32);
+            const int TILE = big ? 64 : 32;
+            const int mb = ceil_div(l + 1, TILE), nb = ceil_div(nmax, TILE);
+            int nslabs = std::max(1, (4 * ctx->sm_count) / (mb * nb));
+            nslabs = std::min(std::min(nslabs, ceil_div(nc, kTP)), kNoAllocMaxSlabs);
+            LArgs a;
+            a.l = l;
+            a.nmax = nmax;
+            a.nslabs = nslabs;
+            a.n = nc;
+            a.r = r;
+            a.x = x;
+            a.ph = ph;
+            a.w = w;
+            a.tab = interpolated ? tab_d + (size_t)l * npts_tab : nullptr;
+            a.npts_tab = npts_tab;
+            a.dx_inv = interpolated ? dxinv[l] : 0.0;
+            a.zmax = interpolated ? zmx[l] : 0.0;
+            a.st1 = st1;
+            a.st2 = st2;
+            a.st0 = st0;
+            a.coef = coef_d + (size_t)l * (l + 1) / 2;
+            a.partial = part_d;
+            a.err = err_d;
+            a.kln = k_ln_dev + (size_t)l * nmax;
+            dim3 grid(nslabs, mb, nb);
+            if (big)
+                k_fp64_raw_l<64><<<grid, kThreads, 3 * kTP * (64 + 1) * sizeof(double), st>>>(a);
+            else
+                k_fp64_raw_l<32><<<grid, kThreads, 3 * kTP * (32 + 1) * sizeof(double), st>>>(a);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            const int cnt = (l + 1) * nmax;
+            double2 *fl = reinterpret_cast<double2 *>(f_lmn_dev) + (size_t)nmax * l * (l + 1) / 2;
+            k_sum_partials<<<ceil_div(cnt, 256), 256, 0, st>>>(part_d, nslabs, cnt, fl);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            double *t = st2;
+            st2 = st1;
+            st1 = st0;
+            st0 = t;
+        }
+    }
+    double wsum = (double)npoints;
+    if (weights_dev && npoints > 0) {
+        k_noalloc_wsum<<<1, 1024, 0, st>>>(weights_dev, npoints, wsum_d);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        CG_CUDA_TRY(cudaMemcpyAsync(&wsum, wsum_d, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    double nf = std::sqrt(2. / kPi) * (4. / 3.) * kPi;  // sfb_raw.cpp:29-30
+    nf *= (double)rmax * rmax * rmax / wsum;
+    catana_status_t s = finish_flmn_cln(f_lmn_dev, nf, lmax, nmax, c_ln_dev, st);
+    if (s != CATANA_OK) return s;
+    int err_h = 0;
+    CG_CUDA_TRY(cudaMemcpyAsync(&err_h, err_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err_h == CATANA_ERR_DOMAIN) {
+        set_error("argument (z) outside of defined range.");
+        return CATANA_ERR_DOMAIN;
+    }
+    return CATANA_OK;
+}
+
+namespace catana_gpu {
 }  // namespace catana_gpu

@@ -98,6 +98,26 @@ catana_status_t catana_gpu_sfb_raw_dev(const double *points_dev, const double *w
                                        double *k_ln_dev, double *c_ln_dev, double *f_lmn_dev,
                                        int *status_dev, catana_gpu_stream_t stream);
 
+/* Allocation-free variant of catana_gpu_sfb_raw_dev (no counterpart in the
+ * reference).  For callers that may not allocate device memory -- code that runs
+ * under a caller-owned memory pool or a fixed memory budget, or that must not
+ * trigger cudaMalloc's implicit device synchronisation -- it runs the plain FP64
+ * raw path with every scratch buffer carved out of one static device array of
+ * 32 MiB per device (held until the process exits) and calls no cudaMalloc,
+ * cudaFree or allocating library routine.  The caller passes device inputs and
+ * device outputs; k_ln_dev, c_ln_dev and f_lmn_dev are required (f_lmn_dev is also
+ * the accumulator).  Plain form only (CATANA_FORM_SPLIT is rejected).  Sizes whose
+ * interpolation tables and partial sums do not fit the array (lmax * nmax above
+ * about 2000 with interpolated j_l -- lmax = nmax = 32 fits, 64 x 64 does not)
+ * return CATANA_ERR_ARG with the reason.  The call
+ * blocks until its results are ready.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress): make it before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race. */
+catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, const double *weights_dev, int64_t npoints,
+                                           uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags,
+                                           double *k_ln_dev, double *c_ln_dev, double *f_lmn_dev,
+                                           catana_gpu_stream_t stream);
+
 /* HEALPix (pixelized) SFB decomposition.  The catalog is given binned: pixel p
  * (RING scheme) holds the radii r_sorted[pix_offsets[p] .. pix_offsets[p+1]), in
  * the order the points were added.  npix = 12 nside^2; pix_offsets has npix+1
