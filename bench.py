@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--rmax", type=float, default=1000.0)
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=600, help="points in the CPU baseline sample")
-    p.add_argument("--plain-sample", type=int, default=100_000, help="points for the FP64 plain GPU comparison")
+    p.add_argument("--plain-sample", type=int, default=20_000, help="points for the FP64 plain GPU comparison")
+    p.add_argument("--side", type=int, default=1, help="also time the FP64 (100k, 32, 32) and HEALPix cases")
     p.add_argument("--no-extras", action="store_true", help="skip e2e/cpu/plain/accuracy legs")
     return p.parse_args()
 
@@ -158,6 +159,78 @@ def run_reference(a):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def side_workloads(torch, _lib, catana, sp):
+    """Two secondary workloads, timed through the public API after the main line:
+    the plain FP64 raw SFB of 100k points uniform in a ball (rmax 1000, lmax = nmax =
+    32, seed 0) on device-resident data, and the HEALPix SFB of 1M points (90% uniform
+    in the ball, 10% in 1000 Gaussian clumps of sigma 5; nside 256, lmax 128, nmax 64,
+    seed 1) including its binning."""
+    res = {}
+    pts, _ = catalog(100000, 1000.0, 0)
+    d_pts = torch.from_numpy(pts).cuda()
+    L, M = 32, 32
+    fc = int(_lib.lib.catana_gpu_flmn_size(L, M))
+    d_k = torch.zeros(L * M, dtype=torch.float64, device="cuda")
+    d_c = torch.zeros_like(d_k)
+    d_f = torch.zeros(2 * fc, dtype=torch.float64, device="cuda")
+
+    def run():
+        _lib.check(_lib.lib.catana_gpu_sfb_raw_dev(ctypes.c_void_p(d_pts.data_ptr()), None, 100000, L, M, 1000.0,
+                                                   _lib.FORM_PLAIN, ctypes.c_void_p(d_k.data_ptr()),
+                                                   ctypes.c_void_p(d_c.data_ptr()), ctypes.c_void_p(d_f.data_ptr()),
+                                                   None, sp), "fp64")
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    _lib.lib.catana_gpu_profile_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    _lib.lib.catana_gpu_profile_enable(0)
+    kms, kn, kfl = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_double()
+    _lib.check(_lib.lib.catana_gpu_profile_report(ctypes.byref(kms), ctypes.byref(kn), ctypes.byref(kfl)))
+    ms = e0.elapsed_time(e1) / 5
+    res["plain_fp64_100k_l32_n32"] = {"value": 100000 * modes(L, M) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+                                     "kernel_k_fp64_raw_l_tflops": kfl.value / (kms.value / 1e3) / 1e12,
+                                     "fp64_peak_note": "nominal GB300 FP64 1.25 TFLOP/s"}
+    # HEALPix
+    rng = np.random.default_rng(1)
+    n, R = 1000000, 1000.0
+    nu = int(0.9 * n)
+    nc = n - nu
+
+    def ball(k):
+        r = R * rng.random(k) ** (1 / 3)
+        ct = rng.uniform(-1, 1, k)
+        ph = rng.uniform(0, 2 * np.pi, k)
+        st = np.sqrt(1 - ct ** 2)
+        return np.stack([r * st * np.cos(ph), r * st * np.sin(ph), r * ct], 1)
+    xyz = [ball(nu)]
+    cen = ball(1000)
+    got = 0
+    while got < nc:
+        p = cen[rng.integers(0, 1000, nc)] + rng.normal(0, 5.0, (nc, 3))
+        p = p[np.sum(p ** 2, 1) < R ** 2][:nc - got]
+        xyz.append(p)
+        got += p.shape[0]
+    pc = catana.PointContainer(np.concatenate(xyz), "cartesian")
+    catana.PixelizedPointContainer(256, pc)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ppc = catana.PixelizedPointContainer(256, pc)
+    tb = time.perf_counter() - t0
+    catana.sfb_decomposition(ppc, 128, 64, R, False, False)
+    t0 = time.perf_counter()
+    catana.sfb_decomposition(ppc, 128, 64, R, False, False)
+    ts = time.perf_counter() - t0
+    res["healpix_nside256_1M_l128_n64"] = {"binning_s": tb, "sfb_s": ts,
+                                           "note": "host API incl. copies; FP64; ring transform is a direct DFT"}
+    return res
 
 
 def workload_config(a):
@@ -267,8 +340,19 @@ def main():
         bound = "fp64"
         kernel = "k_fp64_raw_l"
     achieved = (kfl.value / (kms.value / 1e3)) / 1e12 if kms.value > 0 else None
+    # DRAM bytes of an average k_split_l launch: the ncu capture of l = 200 on 300k points
+    # (profiles/k_split_l_l200_300k_full.md) read+wrote 808 MB = 1.09 x the algorithmic
+    # 12 B per (point, m) of Legendre rows + 48 B per point; scaled here to this run's
+    # chunk size and averaged over l.
+    traffic = None
+    if a.form == "split":
+        chunk = min(a.points, int(16e9 / (12.0 * L)))
+        avg = sum((12.0 * (l + 1) + 48.0) * chunk for l in range(L)) / L
+        traffic = 1.09 * avg
     roof = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": (achieved / peak) if achieved else None, "traffic": None, "peak_source": peak_note,
+            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "traffic_unit": "bytes per launch (average over l), from one ncu capture scaled by points",
+            "peak_source": peak_note,
             "kernel_ms_per_step": kms.value / a.steps, "kernel_launches_per_step": int(kn.value) // max(1, a.steps),
             "kernel_share_of_step": (kms.value / ms_total) if ms_total > 0 else None,
             "algo_flops_per_point_mode": 4}
@@ -295,49 +379,56 @@ def main():
         out["e2e"] = {"value": a.points * nmodes / e2e_t, "unit": UNIT, "ms_per_step": e2e_t * 1e3,
                       "h2d_bytes_per_step": a.points * 32, "d2h_bytes_per_step": 2 * L * M * 8,
                       "api": "catana_gpu_sfb_raw (host buffers, pinned)"}
-        # ---- FP64 plain GPU path on a subsample, and split-vs-plain accuracy ----
+        # ---- FP64 plain GPU path (the drop-in, the reference's default j_l rule) on a subsample ----
         ns = min(a.plain_sample, a.points)
         sub = np.ascontiguousarray(pts[:ns])
         wsub = np.ascontiguousarray(w[:ns])
         fc = int(_lib.lib.catana_gpu_flmn_size(L, M))
-        res = {}
-        for name, fl in (("plain", _lib.FORM_PLAIN | _lib.JL_EXACT), ("split", _lib.FORM_SPLIT)):
+
+        def host_call(fl, store):
             k2 = np.zeros(L * M)
             c2 = np.zeros(L * M)
-            f2 = np.zeros(2 * fc)
+            f2 = np.zeros(2 * fc) if store else None
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             _lib.check(_lib.lib.catana_gpu_sfb_raw(_lib.ptr(sub), _lib.ptr(wsub), ns, L, M, a.rmax, fl, _lib.ptr(k2),
-                                                   _lib.ptr(c2), _lib.ptr(f2), sp), name)
-            res[name] = (time.perf_counter() - t0, c2, f2)
-        tp = res["plain"][0]
-        cp_, fp_ = res["plain"][1], res["plain"][2]
-        cs_, fs_ = res["split"][1], res["split"][2]
-        fpz = fp_[0::2] + 1j * fp_[1::2]
-        fsz_ = fs_[0::2] + 1j * fs_[1::2]
+                                                   _lib.ptr(c2), _lib.ptr(f2), sp), "sfb_raw")
+            return time.perf_counter() - t0, c2, f2
+
+        host_call(_lib.FORM_PLAIN | _lib.JL_AUTO, False)  # builds the cached tables
+        tp = host_call(_lib.FORM_PLAIN | _lib.JL_AUTO, False)[0]
         out["plain_fp64"] = {"value": ns * nmodes / tp, "unit": UNIT, "sample_points": ns,
-                             "note": "FP64 CUDA-core path, exact j_l, host-buffer call incl. copies"}
+                             "note": "FP64 CUDA-core path, interpolated j_l (the reference's rule for N > 1000), "
+                                     "host-buffer call incl. copies, same lmax/nmax/weights"}
         if a.form == "split":
             out["split_vs_plain_speedup"] = value / out["plain_fp64"]["value"]
-        rel = np.abs(cs_ - cp_) / np.abs(cp_)
-        cpm = cp_.reshape(L, M)
-        typ = np.abs(cs_ - cp_).reshape(L, M) / np.maximum(np.abs(cpm), np.median(cpm, axis=1, keepdims=True))
-        rms_l = []
-        off = 0
-        for l in range(L):
-            sl = slice(off, off + (l + 1) * M)
-            rms_l.append(np.sqrt(np.mean(np.abs(fsz_[sl] - fpz[sl]) ** 2) / np.mean(np.abs(fpz[sl]) ** 2)))
-            off += (l + 1) * M
-        out["accuracy_vs_fp64"] = {"sample_points": ns, "reference": "FP64 plain GPU path, exact j_l",
-                                   "c_ln_rel_err_median": float(np.median(rel)),
-                                   "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
-                                   "c_ln_rel_err_max": float(rel.max()),
-                                   "c_ln_abs_err_over_max_c_or_median_c_l_max": float(typ.max()),
-                                   "f_lmn_max_abs_err_over_max_f": float(np.max(np.abs(fsz_ - fpz)) /
-                                                                         np.max(np.abs(fpz))),
-                                   "f_lmn_rms_err_over_rms_f_by_l": {"l=0": float(rms_l[0]),
-                                                                     "l=%d" % (L // 2): float(rms_l[L // 2]),
-                                                                     "l=%d" % (L - 1): float(rms_l[-1])}}
+            # split vs FP64 with exact j_l (the split form's own j_l tables are ~1e-7 accurate)
+            _, cp_, fp_ = host_call(_lib.FORM_PLAIN | _lib.JL_EXACT, True)
+            _, cs_, fs_ = host_call(_lib.FORM_SPLIT, True)
+            fpz = fp_[0::2] + 1j * fp_[1::2]
+            fsz_ = fs_[0::2] + 1j * fs_[1::2]
+            rel = np.abs(cs_ - cp_) / np.abs(cp_)
+            cpm = cp_.reshape(L, M)
+            typ = np.abs(cs_ - cp_).reshape(L, M) / np.maximum(np.abs(cpm), np.median(cpm, axis=1, keepdims=True))
+            rms_l = []
+            off = 0
+            for l in range(L):
+                sl = slice(off, off + (l + 1) * M)
+                rms_l.append(np.sqrt(np.mean(np.abs(fsz_[sl] - fpz[sl]) ** 2) / np.mean(np.abs(fpz[sl]) ** 2)))
+                off += (l + 1) * M
+            out["accuracy_vs_fp64"] = {"sample_points": ns, "reference": "FP64 plain GPU path, exact j_l",
+                                       "c_ln_rel_err_median": float(np.median(rel)),
+                                       "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
+                                       "c_ln_rel_err_max": float(rel.max()),
+                                       "c_ln_abs_err_over_max_c_or_median_c_l_max": float(typ.max()),
+                                       "f_lmn_max_abs_err_over_max_f": float(np.max(np.abs(fsz_ - fpz)) /
+                                                                             np.max(np.abs(fpz))),
+                                       "f_lmn_rms_err_over_rms_f_by_l": {"l=0": float(rms_l[0]),
+                                                                         "l=%d" % (L // 2): float(rms_l[L // 2]),
+                                                                         "l=%d" % (L - 1): float(rms_l[-1])}}
+        # ---- side workloads: FP64 plain at 100k points / lmax = nmax = 32, HEALPix nside 256 ----
+        if a.side:
+            out["side"] = side_workloads(torch, _lib, catana, sp)
         # ---- CPU baseline: the oracle's OpenMP restatement on a bounded sample ----
         cs = min(a.cpu_sample, a.points)
         v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
