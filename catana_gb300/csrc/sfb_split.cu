@@ -54,7 +54,8 @@ namespace {
 constexpr int KT = 32;              // points per tile (two K=16 MMA steps)
 constexpr int NTHR = 512;           // 16 warps
 constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
-constexpr int FLUSH_FOLDS = 32;     // tiles folded into the TMEM sum before it goes to global memory
+constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
+constexpr int FLUSH_FOLDS = 32;     // folds into the TMEM sum before it goes to global memory
 constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
 constexpr double H = 0.5;           // table interval width in z
 constexpr int SPLIT_LMAX = 256;     // scaled-row range limit (see header comment)
@@ -93,6 +94,7 @@ static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 
 struct SplitArgs {
     int l, nmax, nint, nblocks;
+    int mblk;           // complex m per block (balanced, multiple of 4, <= MBLK)
     int64_t n;          // points in the chunk
     int stride;         // row stride of the Legendre rows (>= n, multiple of 32)
     int tiles_per_cta;  // slab length in tiles
@@ -140,8 +142,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int l = a.l;
-    const int mb0 = blockIdx.y * MBLK;
-    const int mcount = min(MBLK, l + 1 - mb0);
+    const int mb0 = blockIdx.y * a.mblk;
+    const int mcount = min(a.mblk, l + 1 - mb0);
     const int ncols = 2 * mcount;
     const int ncols_pad = (ncols + 15) & ~15;
     uint32_t half_cols = 32;
@@ -175,16 +177,18 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const int stride = a.stride;
     float *partial_cta = a.partial + ((size_t)blockIdx.x * a.nblocks + blockIdx.y) * 256 * 128;
 
-    uint32_t uses[2] = {0, 0}, waited[2] = {0, 0};
+    uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
     bool acc_fresh = true;   // next fold overwrites D_acc
     bool first_flush = true; // partial rows not yet written by this CTA
     int folds = 0;
     bool ok = true;
 
     auto wait_buf = [&](int b) -> bool {
-        while (waited[b] < uses[b]) {
-            if (!tc05::mbar_wait(&mbar[b], waited[b] & 1, WAIT_NS)) return false;
-            ++waited[b];
+        uint32_t &wt = b ? waited1 : waited0;
+        const uint32_t us = b ? uses1 : uses0;
+        while (wt < us) {
+            if (!tc05::mbar_wait(&mbar[b], wt & 1, WAIT_NS)) return false;
+            ++wt;
         }
         return true;
     };
@@ -377,8 +381,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             }
         }
         tc05::fence_proxy_async();
-        // ---- fold the previous tile's product into D_acc (needs its MMAs complete) ----
-        if (t > t0) {
+        // ---- every FOLD_TILES tiles: fold the tensor-core sum into D_acc (needs its MMAs complete) ----
+        const bool fold_now = (t > t0) && ((t - t0) % FOLD_TILES == 0);
+        if (fold_now) {
             const int pb = b ^ 1;
             const int f_ok = wait_buf(pb) ? 1 : 0;
             if (!__syncthreads_and(f_ok)) {
@@ -391,7 +396,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         tc05::fence_before();
         __syncthreads();
         tc05::fence_after();
-        // ---- hand tile t to the tensor cores: D_tile = Jhi Yhi + Jhi Ylo + Jlo Yhi ----
+        // ---- hand tile t to the tensor cores: D_tile (+)= Jhi Yhi + Jhi Ylo + Jlo Yhi ----
+        const bool fresh_tile = ((t - t0) % FOLD_TILES == 0);  // D_tile was folded (or never used)
         if (tid == 0) {
             const uint32_t sj_hi = tc05::smem_u32(jhi), sj_lo = tc05::smem_u32(jlo);
             const uint32_t sy_hi = tc05::smem_u32(yhi), sy_lo = tc05::smem_u32(ylo);
@@ -401,13 +407,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                 const uint64_t al = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
                 const uint64_t bh = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
                 const uint64_t bl = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
-                tc05::mma_f16(d_tile, ah, bh, idesc, ks == 0 ? 0u : 1u);
+                tc05::mma_f16(d_tile, ah, bh, idesc, (ks == 0 && fresh_tile) ? 0u : 1u);
                 tc05::mma_f16(d_tile, ah, bl, idesc, 1u);
                 tc05::mma_f16(d_tile, al, bh, idesc, 1u);
             }
             tc05::commit(&mbar[b]);
         }
-        ++uses[b];
+        if (b) ++uses1; else ++uses0;
     }
     // last tile: fold and flush
     if (ok && t1 > t0) {
@@ -436,13 +442,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     if (warp == 0) tc05::tmem_dealloc(tmem, tcols);
 }
 
-// f_acc[l][m][n] += k_ln[n] * sum_slab partial[slab][m / 128][2 (m % 128) + ri][n]  (FP64, slab order)
-__global__ void k_split_reduce(const float *__restrict__ partial, int nslabs, int nblocks, int lp1, int nmax,
-                               const double *__restrict__ kln_row, double2 *__restrict__ fl) {
+// f_acc[l][m][n] += k_ln[n] * sum_slab partial[slab][m / mblk][2 (m % mblk) + ri][n]  (FP64, slab order)
+__global__ void k_split_reduce(const float *__restrict__ partial, int nslabs, int nblocks, int mblk, int lp1,
+                               int nmax, const double *__restrict__ kln_row, double2 *__restrict__ fl) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (m, n)
     if (t >= lp1 * nmax) return;
     const int m = t / nmax, n = t - m * nmax;
-    const int blk = m / MBLK, ml = m - blk * MBLK;
+    const int blk = m / mblk, ml = m - blk * mblk;
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < nslabs; ++s) {
         const float *p = partial + ((size_t)s * nblocks + blk) * 256 * 128;
@@ -759,6 +765,7 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
         float *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
         for (int l = 0; l < lmax; ++l) {
             const int nblocks = (l + 1 + MBLK - 1) / MBLK;
+            const int mblk = (((l + 1 + nblocks - 1) / nblocks) + 3) & ~3;  // balanced, multiple of 4
             const int nslabs = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count / nblocks, ntiles));
             const int tpc = (int)((ntiles + nslabs - 1) / nslabs);
             SplitArgs a;
@@ -766,6 +773,7 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
             a.nmax = nmax;
             a.nint = nint;
             a.nblocks = nblocks;
+            a.mblk = mblk;
             a.n = nc;
             a.stride = (int)stride;
             a.tiles_per_cta = tpc;
@@ -787,7 +795,7 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
             CG_CUDA_TRY(cudaGetLastError());
             const int cnt = (l + 1) * nmax;
             double2 *fl = reinterpret_cast<double2 *>(f_acc_dev) + (size_t)nmax * l * (l + 1) / 2;
-            k_split_reduce<<<ceil_div(cnt, 128), 128, 0, st>>>(partial, nslabs, nblocks, l + 1, nmax,
+            k_split_reduce<<<ceil_div(cnt, 128), 128, 0, st>>>(partial, nslabs, nblocks, mblk, l + 1, nmax,
                                                               kln_dev + (size_t)l * nmax, fl);
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
