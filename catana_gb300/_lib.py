@@ -30,12 +30,24 @@ OK, ERR_ARG, ERR_DOMAIN, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED = range(6)
 JL_AUTO, JL_INTERP, JL_EXACT = 0, 1, 2
 FORM_PLAIN, FORM_SPLIT = 0, 4
 HEALPIX_CONJ_FIX = 8
+BATCH_NO_GRAPH = 16
+
+
+class Catalog(ctypes.Structure):
+    """catana_catalog_t: one catalog of a batched decomposition."""
+    _fields_ = [("points", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("npoints", ctypes.c_int64),
+                ("rmax", ctypes.c_double), ("kmax", ctypes.c_double), ("k_ln", ctypes.c_void_p),
+                ("c_ln", ctypes.c_void_p), ("f_lmn", ctypes.c_void_p), ("lmax", ctypes.c_uint16),
+                ("nmax", ctypes.c_uint16), ("reserved", ctypes.c_uint32)]
 
 SIGNATURES = {
     "catana_gpu_flmn_size": (ctypes.c_size_t, [_U16, _U16]),
     "catana_gpu_sfb_raw": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_sfb_raw_dev": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P, _P]),
     "catana_gpu_sfb_raw_noalloc": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
+    "catana_gpu_sfb_raw_batched": (ctypes.c_int, [_P, _I32, _U32, _D, _P]),
+    "catana_gpu_sfb_raw_batched_dev": (ctypes.c_int, [_P, _I32, _U32, _D, _P, _P]),
+    "catana_gpu_batch_waves": (ctypes.c_double, []),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_bin_points": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
     "catana_gpu_ang2pix_ring": (ctypes.c_int, [_I64, _P, _P, _I64, _P, _P]),

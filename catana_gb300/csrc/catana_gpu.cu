@@ -285,6 +285,133 @@ catana_status_t raw_device(DeviceContext *ctx, const double *pts_d, const double
     return finish_flmn_cln(facc, nf, lmax, nmax, cln_d, st);
 }
 
+// Zero the f entries of modes with k_ln > kmax (plain form of the kmax cut).
+__global__ void k_kcut(double2 *f, const double *kln, int nmax, double kmax) {
+    const int l = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (l + 1) * nmax) return;
+    const int n = t % nmax;
+    if (kln[(size_t)l * nmax + n] > kmax) f[(size_t)nmax * l * (l + 1) / 2 + t] = make_double2(0.0, 0.0);
+}
+
+catana_status_t check_catalogs(const catana_catalog_t *cats, int32_t ncat) {
+    if (ncat < 0 || (ncat > 0 && !cats)) {
+        set_error("ncat must be >= 0 and cats non-null");
+        return CATANA_ERR_ARG;
+    }
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        catana_status_t s = check_args(C.npoints, C.lmax, C.nmax, C.rmax);
+        if (s != CATANA_OK) return s;
+        if ((C.npoints > 0 && !C.points) || ((size_t)C.lmax * C.nmax && (!C.k_ln || !C.c_ln))) {
+            set_error("catalog " + std::to_string(c) + ": null buffer");
+            return CATANA_ERR_ARG;
+        }
+        if (!(C.kmax >= 0.0) || std::isinf(C.kmax)) {
+            set_error("catalog " + std::to_string(c) + ": kmax must be >= 0 and finite (0 = no cut)");
+            return CATANA_ERR_ARG;
+        }
+    }
+    return CATANA_OK;
+}
+
+// Core of both batched entry points: device pointers in the records.
+catana_status_t batched_device(DeviceContext *ctx, const catana_catalog_t *cats, int ncat, uint32_t flags,
+                               double waves, int *err_d, cudaStream_t st) {
+    const bool split = (flags & CATANA_FORM_MASK) == CATANA_FORM_SPLIT;
+    if (split && (ctx->cc_major != 10 || ctx->cc_minor != 3)) {
+        set_error("the split (tcgen05) form needs an sm_103 device");
+        return CATANA_ERR_UNSUPPORTED;
+    }
+    // k_ln (host, cached zeros) and zeroed accumulators; internal f where none is given
+    size_t fin = 0;
+    for (int c = 0; c < ncat; ++c)
+        if (!cats[c].f_lmn) fin += catana_gpu_flmn_size(cats[c].lmax, cats[c].nmax) * 2;
+    if (fin) CG_CUDA_TRY(ctx->flmn.ensure(fin * sizeof(double)));
+    std::vector<double *> facc(ncat);
+    std::vector<std::vector<double>> kh(ncat);
+    size_t fo = 0;
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        const size_t fc = catana_gpu_flmn_size(C.lmax, C.nmax) * 2;
+        facc[c] = C.f_lmn ? C.f_lmn : ctx->flmn.as<double>() + fo;
+        if (!C.f_lmn) fo += fc;
+        kh[c].resize((size_t)C.lmax * C.nmax);
+        kln_table(C.lmax, C.nmax, C.rmax, kh[c].data());
+        if (!kh[c].empty())
+            CG_CUDA_TRY(cudaMemcpyAsync(C.k_ln, kh[c].data(), kh[c].size() * sizeof(double), cudaMemcpyHostToDevice,
+                                        st));
+        if (fc) CG_CUDA_TRY(cudaMemsetAsync(facc[c], 0, fc * sizeof(double), st));
+    }
+    catana_status_t s;
+    if (split) {
+        // catalogs whose Legendre rows exceed 16 GB enter as chunks (same accumulator)
+        std::vector<SplitCatInput> v;
+        for (int c = 0; c < ncat; ++c) {
+            const catana_catalog_t &C = cats[c];
+            if (C.npoints == 0 || C.lmax == 0 || C.nmax == 0) continue;
+            const int64_t chunk =
+                std::max<int64_t>(32, std::min<int64_t>(C.npoints, (int64_t)(16e9 / (12.0 * C.lmax))));
+            for (int64_t p0 = 0; p0 < C.npoints; p0 += chunk) {
+                SplitCatInput in;
+                in.pts = C.points + 3 * p0;
+                in.w = C.weights ? C.weights + p0 : nullptr;
+                in.n = std::min(chunk, C.npoints - p0);
+                in.lmax = C.lmax;
+                in.nmax = C.nmax;
+                in.rmax = C.rmax;
+                in.kmax = C.kmax;
+                in.kln_dev = C.k_ln;
+                in.f_acc = facc[c];
+                v.push_back(in);
+            }
+        }
+        s = split_run(ctx, v, !(flags & CATANA_BATCH_NO_GRAPH), waves, err_d, st);
+        if (s != CATANA_OK) return s;
+    } else {
+        for (int c = 0; c < ncat; ++c) {
+            const catana_catalog_t &C = cats[c];
+            s = fp64_raw_accumulate(ctx, C.points, C.weights, C.npoints, C.lmax, C.nmax,
+                                    resolve_interp(flags, C.npoints), C.k_ln, facc[c], err_d, st);
+            if (s != CATANA_OK) return s;
+            if (C.kmax > 0.0 && C.lmax > 0 && C.nmax > 0) {
+                k_kcut<<<dim3(ceil_div((int64_t)C.lmax * C.nmax, 256), C.lmax), 256, 0, st>>>(
+                    reinterpret_cast<double2 *>(facc[c]), C.k_ln, C.nmax, C.kmax);
+                count_launch();
+                CG_CUDA_TRY(cudaGetLastError());
+            }
+        }
+    }
+    // weight sums (one read-back for all catalogs), then normalise and form C_ln
+    std::vector<double> wsum(ncat);
+    bool any_w = false;
+    for (int c = 0; c < ncat; ++c) {
+        wsum[c] = (double)cats[c].npoints;
+        any_w |= (cats[c].weights && cats[c].npoints > 0);
+    }
+    if (any_w) {
+        CG_CUDA_TRY(ctx->cat_scratch.ensure((size_t)8 * ncat));
+        double *ws = ctx->cat_scratch.as<double>();
+        for (int c = 0; c < ncat; ++c)
+            if (cats[c].weights && cats[c].npoints > 0) {
+                k_wsum<<<1, 1024, 0, st>>>(cats[c].weights, cats[c].npoints, ws + c);
+                count_launch();
+            }
+        CG_CUDA_TRY(cudaGetLastError());
+        std::vector<double> wh(ncat);
+        CG_CUDA_TRY(cudaMemcpyAsync(wh.data(), ws, (size_t)8 * ncat, cudaMemcpyDeviceToHost, st));
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int c = 0; c < ncat; ++c)
+            if (cats[c].weights && cats[c].npoints > 0) wsum[c] = wh[c];
+    }
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        s = finish_flmn_cln(facc[c], norm_factor(C.rmax, wsum[c]), C.lmax, C.nmax, C.c_ln, st);
+        if (s != CATANA_OK) return s;
+    }
+    return CATANA_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -412,6 +539,101 @@ catana_status_t catana_gpu_sfb_raw(const double *points, const double *weights, 
         return CATANA_ERR_DOMAIN;
     }
     return CATANA_OK;
+}
+
+catana_status_t catana_gpu_sfb_raw_batched_dev(const catana_catalog_t *cats, int32_t ncat, uint32_t flags,
+                                               double waves, int *status_dev, catana_gpu_stream_t stream) {
+    catana_status_t s = check_catalogs(cats, ncat);
+    if (s != CATANA_OK || ncat == 0) return s;
+    int cs;
+    DeviceContext *ctx = get_context(&cs);
+    if (!ctx) return (catana_status_t)cs;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int *err_d = status_dev;
+    if (!err_d) {
+        CG_CUDA_TRY(ctx->misc.ensure(256));
+        err_d = ctx->misc.as<int>();
+        CG_CUDA_TRY(cudaMemsetAsync(err_d, 0, sizeof(int), st));
+    }
+    return batched_device(ctx, cats, ncat, flags, waves, err_d, st);
+}
+
+catana_status_t catana_gpu_sfb_raw_batched(const catana_catalog_t *cats, int32_t ncat, uint32_t flags, double waves,
+                                           catana_gpu_stream_t stream) {
+    catana_status_t s = check_catalogs(cats, ncat);
+    if (s != CATANA_OK || ncat == 0) return s;
+    int cs;
+    DeviceContext *ctx = get_context(&cs);
+    if (!ctx) return (catana_status_t)cs;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // staging: inputs packed into io_points, outputs into io_out (256-byte aligned pieces)
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t in_bytes = 0, out_bytes = 0;
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        in_bytes += al((size_t)C.npoints * 3 * sizeof(double)) + (C.weights ? al((size_t)C.npoints * sizeof(double)) : 0);
+        const size_t lm = (size_t)C.lmax * C.nmax;
+        out_bytes += 2 * al(lm * sizeof(double)) + al(catana_gpu_flmn_size(C.lmax, C.nmax) * 2 * sizeof(double));
+    }
+    CG_CUDA_TRY(ctx->io_points.ensure(in_bytes + 256));
+    CG_CUDA_TRY(ctx->io_out.ensure(out_bytes + 256));
+    CG_CUDA_TRY(ctx->misc.ensure(256));
+    int *err_d = ctx->misc.as<int>();
+    CG_CUDA_TRY(cudaMemsetAsync(err_d, 0, sizeof(int), st));
+    std::vector<catana_catalog_t> dc(cats, cats + ncat);
+    char *ip = ctx->io_points.as<char>(), *op = ctx->io_out.as<char>();
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        const size_t pb = (size_t)C.npoints * 3 * sizeof(double), wb = (size_t)C.npoints * sizeof(double);
+        dc[c].points = reinterpret_cast<const double *>(ip);
+        if (pb) CG_CUDA_TRY(cudaMemcpyAsync(ip, C.points, pb, cudaMemcpyHostToDevice, st));
+        ip += al(pb);
+        if (C.weights) {
+            dc[c].weights = reinterpret_cast<const double *>(ip);
+            if (wb) CG_CUDA_TRY(cudaMemcpyAsync(ip, C.weights, wb, cudaMemcpyHostToDevice, st));
+            ip += al(wb);
+        }
+        const size_t lmb = (size_t)C.lmax * C.nmax * sizeof(double);
+        dc[c].k_ln = reinterpret_cast<double *>(op);
+        op += al(lmb);
+        dc[c].c_ln = reinterpret_cast<double *>(op);
+        op += al(lmb);
+        dc[c].f_lmn = reinterpret_cast<double *>(op);
+        op += al(catana_gpu_flmn_size(C.lmax, C.nmax) * 2 * sizeof(double));
+    }
+    s = batched_device(ctx, dc.data(), ncat, flags, waves, err_d, st);
+    if (s != CATANA_OK) return s;
+    int err_h = 0;
+    CG_CUDA_TRY(cudaMemcpyAsync(&err_h, err_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    for (int c = 0; c < ncat; ++c) {
+        const catana_catalog_t &C = cats[c];
+        const size_t lmb = (size_t)C.lmax * C.nmax * sizeof(double);
+        if (lmb) {
+            CG_CUDA_TRY(cudaMemcpyAsync(C.k_ln, dc[c].k_ln, lmb, cudaMemcpyDeviceToHost, st));
+            CG_CUDA_TRY(cudaMemcpyAsync(C.c_ln, dc[c].c_ln, lmb, cudaMemcpyDeviceToHost, st));
+        }
+        if (C.f_lmn && lmb)
+            CG_CUDA_TRY(cudaMemcpyAsync(C.f_lmn, dc[c].f_lmn, catana_gpu_flmn_size(C.lmax, C.nmax) * 2 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err_h == CATANA_ERR_DOMAIN) {
+        set_error("argument (z) outside of defined range.");
+        return CATANA_ERR_DOMAIN;
+    }
+    if (err_h != 0) {
+        set_error("split kernel reported a timed-out wait");
+        return CATANA_ERR_CUDA;
+    }
+    return CATANA_OK;
+}
+
+double catana_gpu_batch_waves(void) {
+    int cs;
+    DeviceContext *ctx = get_context(&cs);
+    return ctx ? ctx->split_last_waves : 0.0;
 }
 
 catana_status_t catana_gpu_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -66,12 +67,17 @@ struct DeviceContext {
     DevBuf kln;        // k_ln on device
     DevBuf coef;       // Legendre recurrence coefficients
     DevBuf tables;     // j_l interpolation tables (FP64 lerp)
-    DevBuf misc;       // error word, small scalars
+    DevBuf misc;       // error word, small scalars (never grown past 256 bytes: callers hold pointers into it)
+    DevBuf cat_scratch;  // per-catalog scalars of batched runs (extents, weight sums)
     DevBuf io_points;  // staging of host inputs
     DevBuf io_out;     // staging of outputs
     DevBuf split_ws;   // split-form workspace
     DevBuf split_tab;  // split-form tables
+    DevBuf split_plan; // split-form plan (catalog descriptors, items, reductions)
     SplitCache split_cache;
+    std::map<std::string, double> split_tuned;  // autotuned waves per catalog set
+    double split_last_waves = 0.0;
+    cudaStream_t capture_stream = nullptr;      // stream the split level loop is captured on
     DevBuf hp_ws;      // HEALPix workspace
     // cache keys
     int coef_lmax = -1;
@@ -109,6 +115,23 @@ catana_status_t finish_flmn_cln(double *f_dev, double norm, int lmax, int nmax, 
 catana_status_t ensure_lerp_tables(DeviceContext *ctx, int lmax, int nmax, cudaStream_t st);
 // Legendre coefficients for l < lmax, cached in ctx->coef.
 catana_status_t ensure_coefs(DeviceContext *ctx, int lmax, cudaStream_t st);
+
+// One catalog of a split-form run (device pointers; f_acc zeroed by the caller).
+struct SplitCatInput {
+    const double *pts = nullptr;  // n x 3 (r, theta, phi)
+    const double *w = nullptr;    // optional weights
+    int64_t n = 0;
+    int lmax = 0, nmax = 0;
+    double rmax = 1.0;
+    double kmax = 0.0;            // > 0: keep only k_ln <= kmax
+    double *kln_dev = nullptr;    // k_ln (lmax x nmax), already on the device
+    double *f_acc = nullptr;      // packed complex f_lmn accumulator
+};
+// Split form over several catalogs: level-synchronous launches over all of them,
+// optionally captured as one CUDA graph.  `waves` = CTAs per SM each level's work
+// items are cut for; <= 0 autotunes it (timed sample levels, cached per catalog set).
+catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats, bool use_graph, double waves,
+                          int *err_dev, cudaStream_t st);
 
 // Split (tensor-core) raw path (sfb_split.cu).
 catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,

@@ -92,21 +92,33 @@ struct SplitPt {
 };
 static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 
+// One catalog (or catalog chunk) of a split-form plan.
+struct SplitCat {
+    const SplitPt *pts;     // radius-sorted point records, padded to whole tiles
+    float *rows;            // three Legendre row sets; set k at rows + k * stride * lrows
+    int64_t n;              // points
+    int stride;             // row stride (multiple of 32, >= n)
+    int lrows;              // rows per set (the catalog's lmax)
+    int kzw;                // row width of kz (the catalog's nmax)
+    int pad_;
+    const float2 *kz;       // [l][kzw]: k_ln / H as float-float
+    const float *jscale;    // [l]: 2^sJ
+    const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
+};
+
+// One CTA of a level launch: a catalog, a block of complex m, a range of tiles.
+struct SplitItem {
+    int cat, mb0, mcount, pad_;
+    int64_t t0, t1;
+};
+
 struct SplitArgs {
-    int l, nmax, nint, nblocks;
-    int mblk;           // complex m per block (balanced, multiple of 4, <= MBLK)
-    int64_t n;          // points in the chunk
-    int stride;         // row stride of the Legendre rows (>= n, multiple of 32)
-    int tiles_per_cta;  // slab length in tiles
-    const SplitPt *pts;           // points of the chunk (sorted by radius)
-    const float *st1, *st2;       // scaled P_{l-1}^m, P_{l-2}^m rows [m][stride]
-    float *st0;                   // scaled P_l^m out
-    const float4 *coef;           // row l, m = 0..l
-    const float2 *kz;             // row l, n < nmax: k_ln / H as float-float
-    const float4 *tab;            // row l: nint intervals x 2 float4 (6 coefficients + pad)
-    float jscale;                 // 2^sJ
-    float inv_scale;              // 1 / (2^sJ * Y_SCALE)  (applied at flush)
-    float *partial;               // [slab][block][256][128]
+    int l, nint;
+    const SplitItem *items;  // this level's items (one per CTA)
+    const SplitCat *cats;
+    const float4 *coef;      // recurrence coefficients, row l
+    const float4 *tab;       // j_l table, row l: nint intervals x 2 float4
+    float *partial;          // [item][256][128]
     int *err;
 };
 
@@ -142,8 +154,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int l = a.l;
-    const int mb0 = blockIdx.y * a.mblk;
-    const int mcount = min(a.mblk, l + 1 - mb0);
+    const SplitItem item = a.items[blockIdx.x];
+    const SplitCat cat = a.cats[item.cat];
+    const int mb0 = item.mb0;
+    const int mcount = item.mcount;
+    const int nmax = cat.nmax_l[l];
+    const float jscale = cat.jscale[l];
+    const float inv_scale = 1.0f / (jscale * Y_SCALE);
     const int ncols = 2 * mcount;
     const int ncols_pad = (ncols + 15) & ~15;
     uint32_t half_cols = 32;
@@ -153,8 +170,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
     float2 *s_kz = reinterpret_cast<float2 *>(sm + OFF_KZ);
     float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);
+    const float2 *kz_row = cat.kz + (size_t)l * cat.kzw;
     for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
-    for (int t = tid; t < a.nmax; t += NTHR) s_kz[t] = a.kz[t];
+    for (int t = tid; t < nmax; t += NTHR) s_kz[t] = kz_row[t];
     for (int t = tid; t < mcount; t += NTHR) s_coef[t] = a.coef[mb0 + t];
     if (tid == 0) {
         tc05::mbar_init(&mbar[0], 1);
@@ -167,15 +185,17 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const uint32_t tmem = tmem_base_sh;
     const uint32_t d_tile = tmem, d_acc = tmem + half_cols;
 
-    const int64_t t0 = (int64_t)blockIdx.x * a.tiles_per_cta;
-    const int64_t ntiles_total = (a.n + KT - 1) / KT;
-    const int64_t t1 = min(ntiles_total, t0 + a.tiles_per_cta);
+    const int64_t t0 = item.t0, t1 = item.t1;
     const int q = lane, g = warp;
     const int MRW = (((mcount + 15) / 16) + 3) & ~3;  // m per warp, multiple of 4 (<= 8)
     const int mlo = g * MRW, mhi = min(mlo + MRW, mcount);  // local m range of this warp
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
-    const int stride = a.stride;
-    float *partial_cta = a.partial + ((size_t)blockIdx.x * a.nblocks + blockIdx.y) * 256 * 128;
+    const int stride = cat.stride;
+    const size_t set = (size_t)stride * cat.lrows;
+    const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
+    const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
+    float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
+    float *partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
     bool acc_fresh = true;   // next fold overwrites D_acc
@@ -201,7 +221,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         // the tile's point records (the buffer is padded to whole tiles)
         if (tid < (int)(SM_STPTS / 16))
             tc05::cp_async16(stg + 2 * SM_STROW + tid * 16,
-                             reinterpret_cast<const uint8_t *>(a.pts + i0) + tid * 16);
+                             reinterpret_cast<const uint8_t *>(cat.pts + i0) + tid * 16);
         if (l == 0) return;
         const int per_set = mcount * 8;  // 16-byte pieces per row set
         for (int c = tid; c < 2 * per_set; c += NTHR) {
@@ -211,7 +231,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             const int m = mb0 + ml;
             if (which && m > l - 2) continue;
             const int msrc = (m == l) ? l - 1 : m;
-            const float *src = (which ? a.st2 : a.st1) + (int64_t)msrc * stride + i0 + part * 4;
+            const float *src = (which ? st2 : st1) + (int64_t)msrc * stride + i0 + part * 4;
             tc05::cp_async16(stg + which * SM_STROW + ml * 128 + part * 16, src);
         }
     };
@@ -246,12 +266,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             uint32_t v[16];
             tc05::tmem_ld16(d_acc + ((uint32_t)(qd * 32) << 16) + gi * 16, v);
             tc05::tmem_wait_ld();
-            if (lane_n < a.nmax) {
+            if (lane_n < nmax) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int col = gi * 16 + j;
                     if (col < ncols) {
-                        const float d = __uint_as_float(v[j]) * a.inv_scale;
+                        const float d = __uint_as_float(v[j]) * inv_scale;
                         float *p = partial_cta + (size_t)col * 128 + lane_n;
                         *p = first_flush ? d : (*p + d);
                     }
@@ -283,14 +303,14 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
                                                                 2 * SM_STROW + q * 48);
         const int64_t i = t * KT + q;
-        const bool valid = i < a.n;
+        const bool valid = i < cat.n;
         // ---- J tile: n = 8 g .. 8 g + 7 ----
         {
             float rh = 0.f, rl = 0.f, wj = 0.f;
             if (valid) {
                 rh = pt.r_hi;
                 rl = pt.r_lo;
-                wj = pt.w * a.jscale;
+                wj = pt.w * jscale;
             }
             const int n0 = 8 * g;
             float v[8];
@@ -298,7 +318,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             for (int k = 0; k < 8; ++k) {
                 const int n = n0 + k;
                 float val = 0.f;
-                if (valid && n < a.nmax) {
+                if (valid && n < nmax) {
                     const float2 kk = s_kz[n];
                     const float p = rh * kk.x;
                     float e = fmaf(rh, kk.x, -p);
@@ -363,7 +383,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                                 const float vv = fmaf(c.y, tt, -bb);
                                 P = fmaf(c.x, tt, vv);
                             }
-                            a.st0[(int64_t)m * stride + i] = P;
+                            st0[(int64_t)m * stride + i] = P;
                             const float Pu = P * Y_UNSCALE;
                             yr = Pu * cm;
                             yi = -Pu * smv;
@@ -442,24 +462,33 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     if (warp == 0) tc05::tmem_dealloc(tmem, tcols);
 }
 
-// f_acc[l][m][n] += k_ln[n] * sum_slab partial[slab][m / mblk][2 (m % mblk) + ri][n]  (FP64, slab order)
-__global__ void k_split_reduce(const float *__restrict__ partial, int nslabs, int nblocks, int mblk, int lp1,
-                               int nmax, const double *__restrict__ kln_row, double2 *__restrict__ fl) {
+// One catalog's reduction at one level: its items are ordered block-major, then slab.
+struct SplitRed {
+    int item0, nslabs, mblk, nmax_l, kzw, pad_;
+    double2 *fl;            // f accumulator block of l: [m][kzw]
+    const double *kln_row;  // k_ln row l (kzw entries)
+};
+
+// f[l][m][n] += k_ln[n] * sum_slab partial[item(m / mblk, slab)][2 (m % mblk) + ri][n]
+// (FP64, slab order); blockIdx.y selects the catalog.
+__global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const SplitRed *__restrict__ reds) {
+    const SplitRed r = reds[blockIdx.y];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (m, n)
-    if (t >= lp1 * nmax) return;
-    const int m = t / nmax, n = t - m * nmax;
-    const int blk = m / mblk, ml = m - blk * mblk;
+    if (t >= lp1 * r.nmax_l) return;
+    const int m = t / r.nmax_l, n = t - m * r.nmax_l;
+    const int blk = m / r.mblk, ml = m - blk * r.mblk;
     double sr = 0.0, si = 0.0;
-    for (int s = 0; s < nslabs; ++s) {
-        const float *p = partial + ((size_t)s * nblocks + blk) * 256 * 128;
+    for (int sl = 0; sl < r.nslabs; ++sl) {
+        const float *p = partial + (size_t)(r.item0 + blk * r.nslabs + sl) * 256 * 128;
         sr += (double)p[(size_t)(2 * ml) * 128 + n];
         si += (double)p[(size_t)(2 * ml + 1) * 128 + n];
     }
-    const double k = kln_row[n];
-    double2 o = fl[t];
-    o.x += k * sr;
-    o.y += k * si;
-    fl[t] = o;
+    const double k = r.kln_row[n];
+    double2 *o = r.fl + (size_t)m * r.kzw + n;
+    double2 v = *o;
+    v.x += k * sr;
+    v.y += k * si;
+    *o = v;
 }
 
 // Point preparation, in radius-sorted order: float-float r, cos(theta), sin(theta);
@@ -600,212 +629,518 @@ std::vector<double> cheb_vandermonde_inverse() {
 
 }  // namespace
 
-catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
-                                     int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
-                                     double *f_acc_dev, int *err_dev, cudaStream_t st) {
-    if (lmax > SPLIT_LMAX || nmax > SPLIT_NMAX) {
-        set_error("the split form supports lmax <= 256 and nmax <= 128");
-        return CATANA_ERR_ARG;
+// ---------------------------------------------------------------------------
+// Host side: a plan of (catalog, level) work items.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct CatPlan {
+    SplitCatInput in;
+    double max_r = 0.0, max_w = 1.0;
+    std::vector<double> kh;     // k_ln row-major [l][nmax]
+    std::vector<int> nmax_l;    // radial orders kept at each l (kmax cut)
+    int64_t stride = 0, ntiles = 0;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// j_l tables for l < lmax over nint intervals (cached; a larger cached table serves)
+catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cudaStream_t st) {
+    SplitCache &C = ctx->split_cache;
+    if (C.lmax >= lmax && C.nint >= nint && C.lmax == (int)C.maxj.size()) return CATANA_OK;
+    lmax = std::max(lmax, C.lmax);
+    nint = std::max(nint, C.nint);
+    const size_t tab_bytes = (size_t)lmax * nint * 2 * sizeof(float4);
+    const size_t coef_bytes = (size_t)lmax * (lmax + 1) / 2 * sizeof(float4);
+    CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + coef_bytes + 1024));
+    const size_t vbytes = (size_t)nint * 6 * lmax * sizeof(double);
+    DevBuf tmp;
+    CG_CUDA_TRY(tmp.ensure(vbytes + 36 * sizeof(double)));
+    double *vals = tmp.as<double>();
+    double *vinv = vals + (size_t)nint * 6 * lmax;
+    std::vector<double> vi = cheb_vandermonde_inverse();
+    CG_CUDA_TRY(cudaMemcpyAsync(vinv, vi.data(), 36 * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_split_nodes<<<ceil_div(nint * 6, 64), 64, 0, st>>>(lmax, nint, vals);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    float4 *tab = ctx->split_tab.as<float4>();
+    k_split_coefs<<<ceil_div((int64_t)lmax * nint, 128), 128, 0, st>>>(lmax, nint, vals, vinv, tab);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    std::vector<float4> co((size_t)lmax * (lmax + 1) / 2);
+    for (int l = 0; l < lmax; ++l)
+        for (int m = 0; m <= l; ++m) {
+            double A = 0.0, B = 0.0;
+            if (l >= 1 && m == l) {
+                A = -std::sqrt((2.0 * l + 1.0) / (2.0 * l));
+            } else if (l >= 1 && m == l - 1) {
+                A = std::sqrt(2.0 * l + 1.0);
+            } else if (l >= 2) {
+                const double dl = l, dl1 = l - 1, mm = (double)m * m;
+                const double aa = std::sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+                const double bb = std::sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
+                A = aa;
+                B = aa * bb;
+            }
+            float ah, al, bh, bl;
+            split_ff(A, ah, al);
+            split_ff(B, bh, bl);
+            co[(size_t)l * (l + 1) / 2 + m] = make_float4(ah, al, bh, bl);
+        }
+    CG_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(tab) + tab_bytes, co.data(), coef_bytes,
+                                cudaMemcpyHostToDevice, st));
+    C.maxj.assign(lmax, 1.0);
+    for (int l = 1; l < lmax; ++l) {  // largest |j_l|: around the first maximum, z ~ l + 0.8 l^(1/3)
+        double mj = 0.0;
+        const double zc = l + 0.8 * std::cbrt((double)l);
+        for (int q = -200; q <= 400; ++q) {
+            const double z = zc + 0.02 * q;
+            if (z > 0) mj = std::max(mj, std::fabs(sbessel_jl(l, z)));
+        }
+        C.maxj[l] = 1.05 * mj;
     }
-    if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    tmp.release();
+    C.lmax = lmax;
+    C.nint = nint;
+    return CATANA_OK;
+}
+
+// autotune cache key: catalog count, sizes and multipoles of a group
+std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
+    std::string k = std::to_string(c1 - c0);
+    for (int c = c0; c < c1; ++c) {
+        k += ':';
+        k += std::to_string((cats[c].in.n + 4095) / 4096);
+        k += '/';
+        k += std::to_string(cats[c].in.lmax);
+    }
+    return k;
+}
+
+}  // namespace
+
+catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_in, bool use_graph,
+                          double waves, int *err_dev, cudaStream_t st) {
+    std::vector<CatPlan> cats;
+    for (auto &c : cats_in) {
+        if (c.lmax > SPLIT_LMAX || c.nmax > SPLIT_NMAX) {
+            set_error("the split form supports lmax <= 256 and nmax <= 128");
+            return CATANA_ERR_ARG;
+        }
+        if (c.n <= 0 || c.lmax == 0 || c.nmax == 0) continue;
+        if (c.n > (int64_t)0xFFFFFFF0ll) {
+            set_error("the split form takes at most 2^32 - 16 points per catalog");
+            return CATANA_ERR_ARG;
+        }
+        CatPlan p;
+        p.in = c;
+        cats.push_back(p);
+    }
+    if (cats.empty()) return CATANA_OK;
     static bool attr = false;
     if (!attr) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
         attr = true;
     }
-    // ---- catalog extent: max r, max |w| ----
-    CG_CUDA_TRY(ctx->misc.ensure(256));
-    unsigned long long *mx = reinterpret_cast<unsigned long long *>(ctx->misc.as<char>() + 128);
-    CG_CUDA_TRY(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
-    k_split_maxes<<<std::min<int64_t>(4 * ctx->sm_count, ceil_div(npoints, 256)), 256, 0, st>>>(points_dev, weights_dev,
-                                                                                           npoints, mx);
-    count_launch();
+    // ---- extents: max r and max |w| per catalog (one synchronisation) ----
+    const int nc = (int)cats.size();
+    CG_CUDA_TRY(ctx->cat_scratch.ensure((size_t)16 * nc));
+    unsigned long long *mx = ctx->cat_scratch.as<unsigned long long>();
+    CG_CUDA_TRY(cudaMemsetAsync(mx, 0, (size_t)16 * nc, st));
+    for (int c = 0; c < nc; ++c) {
+        const int64_t n = cats[c].in.n;
+        k_split_maxes<<<std::min<int64_t>(4 * ctx->sm_count, ceil_div(n, 256)), 256, 0, st>>>(cats[c].in.pts,
+                                                                                             cats[c].in.w, n,
+                                                                                             mx + 2 * c);
+        count_launch();
+    }
     CG_CUDA_TRY(cudaGetLastError());
-    unsigned long long mxh[2];
-    CG_CUDA_TRY(cudaMemcpyAsync(mxh, mx, sizeof(mxh), cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned long long> mxh(2 * nc);
+    CG_CUDA_TRY(cudaMemcpyAsync(mxh.data(), mx, (size_t)16 * nc, cudaMemcpyDeviceToHost, st));
     CG_CUDA_TRY(cudaStreamSynchronize(st));
-    double max_r, max_w;
-    memcpy(&max_r, &mxh[0], 8);
-    memcpy(&max_w, &mxh[1], 8);
-    if (!(max_w > 0.0)) max_w = 1.0;
-    // ---- k_ln (host copy), table extent ----
-    std::vector<double> kh((size_t)lmax * nmax);
-    kln_table(lmax, nmax, rmax, kh.data());
+    int lmax_all = 0;
     double zmax = 0.0;
-    for (int l = 0; l < lmax; ++l) zmax = std::max(zmax, kh[(size_t)l * nmax + nmax - 1] * max_r);
+    for (int c = 0; c < nc; ++c) {
+        CatPlan &P = cats[c];
+        memcpy(&P.max_r, &mxh[2 * c], 8);
+        memcpy(&P.max_w, &mxh[2 * c + 1], 8);
+        if (!(P.max_w > 0.0)) P.max_w = 1.0;
+        const int L = P.in.lmax, M = P.in.nmax;
+        P.kh.resize((size_t)L * M);
+        kln_table(L, M, P.in.rmax, P.kh.data());
+        P.nmax_l.assign(L, M);
+        for (int l = 0; l < L; ++l) {
+            int k = M;
+            if (P.in.kmax > 0.0) {
+                k = 0;
+                while (k < M && P.kh[(size_t)l * M + k] <= P.in.kmax) ++k;
+            }
+            P.nmax_l[l] = k;
+            if (k > 0) zmax = std::max(zmax, P.kh[(size_t)l * M + k - 1] * P.max_r);
+        }
+        lmax_all = std::max(lmax_all, L);
+        P.stride = (P.in.n + 31) / 32 * 32;
+        P.ntiles = (P.in.n + KT - 1) / KT;
+    }
     const int nint = (int)std::ceil(zmax / H) + 1;
     if (nint > NINT_MAX) {
         set_error("split form: k_ln * max(r) exceeds the resident j_l table (max r beyond rmax?)");
         return CATANA_ERR_DOMAIN;
     }
-    // ---- tables (cached per lmax, nmax, nint) ----
-    SplitCache &C = ctx->split_cache;
-    const size_t tab_bytes = (size_t)lmax * nint * 2 * sizeof(float4);
-    const size_t coef_bytes = (size_t)lmax * (lmax + 1) / 2 * sizeof(float4);
-    const size_t kz_bytes = (size_t)lmax * nmax * sizeof(float2);
-    if (C.lmax != lmax || C.nmax != nmax || C.nint != nint) {
-        CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + coef_bytes + kz_bytes + 1024));
-        // node values (temporary, in the partial buffer's allocation)
-        const size_t vbytes = (size_t)nint * 6 * lmax * sizeof(double);
-        CG_CUDA_TRY(ctx->partial.ensure(vbytes + 36 * sizeof(double)));
-        double *vals = ctx->partial.as<double>();
-        double *vinv = vals + (size_t)nint * 6 * lmax;
-        std::vector<double> vi = cheb_vandermonde_inverse();
-        CG_CUDA_TRY(cudaMemcpyAsync(vinv, vi.data(), 36 * sizeof(double), cudaMemcpyHostToDevice, st));
-        k_split_nodes<<<ceil_div(nint * 6, 64), 64, 0, st>>>(lmax, nint, vals);
-        count_launch();
-        CG_CUDA_TRY(cudaGetLastError());
-        float4 *tab = ctx->split_tab.as<float4>();
-        k_split_coefs<<<ceil_div((int64_t)lmax * nint, 128), 128, 0, st>>>(lmax, nint, vals, vinv, tab);
-        count_launch();
-        CG_CUDA_TRY(cudaGetLastError());
-        // recurrence coefficients (A = a_lm, B = a_lm b_lm; sectoral and m = l-1 specials)
-        std::vector<float4> co((size_t)lmax * (lmax + 1) / 2);
-        for (int l = 0; l < lmax; ++l)
-            for (int m = 0; m <= l; ++m) {
-                double A = 0.0, B = 0.0;
-                if (l >= 1 && m == l) {
-                    A = -std::sqrt((2.0 * l + 1.0) / (2.0 * l));
-                } else if (l >= 1 && m == l - 1) {
-                    A = std::sqrt(2.0 * l + 1.0);
-                } else if (l >= 2) {
-                    const double dl = l, dl1 = l - 1, mm = (double)m * m;
-                    const double aa = std::sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
-                    const double bb = std::sqrt((dl1 * dl1 - mm) / (4.0 * dl1 * dl1 - 1.0));
-                    A = aa;
-                    B = aa * bb;
-                }
-                float ah, al, bh, bl;
-                split_ff(A, ah, al);
-                split_ff(B, bh, bl);
-                co[(size_t)l * (l + 1) / 2 + m] = make_float4(ah, al, bh, bl);
-            }
-        float4 *coef_d = reinterpret_cast<float4 *>(reinterpret_cast<char *>(tab) + tab_bytes);
-        CG_CUDA_TRY(cudaMemcpyAsync(coef_d, co.data(), coef_bytes, cudaMemcpyHostToDevice, st));
-        C.maxj.assign(lmax, 1.0);
-        for (int l = 0; l < lmax; ++l) {
-            // largest |j_l| on [0, zmax]: sample around the first maximum (z ~ l + 0.8 l^(1/3))
-            double mj = (l == 0) ? 1.0 : 0.0;
-            if (l > 0) {
-                const double zc = l + 0.8 * std::cbrt((double)l);
-                for (int s = -200; s <= 400; ++s) {
-                    const double z = zc + 0.02 * s;
-                    if (z > 0) mj = std::max(mj, std::fabs(sbessel_jl(l, z)));
-                }
-                mj *= 1.05;
-            }
-            C.maxj[l] = mj;
-        }
-        CG_CUDA_TRY(cudaStreamSynchronize(st));
-        C.lmax = lmax;
-        C.nmax = nmax;
-        C.nint = nint;
-    }
-    // per call: k as float-float, scaled by 1/H (depends on rmax)
+    catana_status_t s = ensure_split_tables(ctx, lmax_all, nint, st);
+    if (s != CATANA_OK) return s;
+    const int nint_tab = ctx->split_cache.nint, lmax_tab = ctx->split_cache.lmax;
     float4 *tab = ctx->split_tab.as<float4>();
-    float4 *coef_d = reinterpret_cast<float4 *>(reinterpret_cast<char *>(tab) + tab_bytes);
-    float2 *kz_d = reinterpret_cast<float2 *>(reinterpret_cast<char *>(coef_d) + coef_bytes);
+    const float4 *coef_d =
+        reinterpret_cast<const float4 *>(reinterpret_cast<char *>(tab) + (size_t)lmax_tab * nint_tab * 2 * sizeof(float4));
+
+    // ---- groups of catalogs whose Legendre rows fit the budget ----
+    const double row_budget = 48e9;
+    std::vector<std::pair<int, int>> groups;  // [begin, end)
     {
-        std::vector<float2> kz((size_t)lmax * nmax);
-        for (size_t t = 0; t < kz.size(); ++t) {
-            float hi, lo;
-            split_ff(kh[t] / H, hi, lo);
-            kz[t] = make_float2(hi, lo);
+        int b = 0;
+        double acc = 0.0;
+        for (int c = 0; c < nc; ++c) {
+            const double need = 3.0 * cats[c].stride * cats[c].in.lmax * 4.0;
+            bool shared = false;  // pieces of one catalog share f: never in one level launch
+            for (int q = b; q < c; ++q) shared |= (cats[q].in.f_acc == cats[c].in.f_acc);
+            if (c > b && (acc + need > row_budget || shared)) {
+                groups.push_back({b, c});
+                b = c;
+                acc = 0.0;
+            }
+            acc += need;
         }
-        CG_CUDA_TRY(cudaMemcpyAsync(kz_d, kz.data(), kz_bytes, cudaMemcpyHostToDevice, st));
+        groups.push_back({b, nc});
     }
-    // J scale per l: a power of two that brings max |w j_l| into [2^14, 2^15): the
-    // typical |J| (j_l ~ 1/z at large z) then keeps a normal FP16 lo half.
-    std::vector<float> jscale(lmax);
-    for (int l = 0; l < lmax; ++l) {
-        const int e = (int)std::floor(std::log2(32768.0 / (C.maxj[l] * max_w)));
-        jscale[l] = (float)std::ldexp(1.0, std::max(-60, std::min(100, e)));
-    }
-
-    // ---- point chunks: sorted point records and three Legendre row sets ----
-    const int64_t chunk = std::max<int64_t>(KT, std::min<int64_t>(npoints, (int64_t)(16e9 / (12.0 * lmax))));
-    const int64_t stride = (chunk + 31) / 32 * 32;
-    auto al256 = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t ptbytes = al256((size_t)stride * sizeof(SplitPt));
-    const size_t keybytes = al256((size_t)stride * sizeof(uint32_t));
-    const size_t histbytes = al256((size_t)256 * ((stride + 4095) / 4096) * sizeof(uint32_t));
-    const size_t rowbytes = al256((size_t)stride * lmax * sizeof(float));
-    CG_CUDA_TRY(ctx->split_ws.ensure(ptbytes + 4 * keybytes + histbytes + 3 * rowbytes));
-    char *ws = ctx->split_ws.as<char>();
-    SplitPt *spts = reinterpret_cast<SplitPt *>(ws);
-    uint32_t *keys = reinterpret_cast<uint32_t *>(ws + ptbytes);
-    uint32_t *perm = reinterpret_cast<uint32_t *>(ws + ptbytes + keybytes);
-    uint32_t *tkeys = reinterpret_cast<uint32_t *>(ws + ptbytes + 2 * keybytes);
-    uint32_t *tvals = reinterpret_cast<uint32_t *>(ws + ptbytes + 3 * keybytes);
-    uint32_t *hist = reinterpret_cast<uint32_t *>(ws + ptbytes + 4 * keybytes);
-    float *rows[3];
-    for (int k = 0; k < 3; ++k)
-        rows[k] = reinterpret_cast<float *>(ws + ptbytes + 4 * keybytes + histbytes + k * rowbytes);
-
-    const int nblocks_max = (lmax + MBLK - 1) / MBLK;
-    const int slabs_max = std::max(1, ctx->sm_count);
-    CG_CUDA_TRY(ctx->partial.ensure((size_t)slabs_max * nblocks_max * 256 * 128 * sizeof(float)));
-    float *partial = ctx->partial.as<float>();
-
-    for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
-        const int64_t nc = std::min(chunk, npoints - c0);
-        const int64_t npad = (nc + KT - 1) / KT * KT;
-        k_split_keys<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, nc, max_r > 0.0 ? 1.0 / max_r : 0.0,
-                                                        keys, perm);
-        count_launch();
-        CG_CUDA_TRY(cudaGetLastError());
-        catana_status_t ss = radix_sort_pairs(keys, perm, tkeys, tvals, nc, 16, hist, st);
-        if (ss != CATANA_OK) return ss;
-        k_split_prep<<<ceil_div(npad, 256), 256, 0, st>>>(points_dev + 3 * c0,
-                                                          weights_dev ? weights_dev + c0 : nullptr, perm, nc, npad,
-                                                          spts, err_dev);
-        count_launch();
-        CG_CUDA_TRY(cudaGetLastError());
-        const int64_t ntiles = (nc + KT - 1) / KT;
-        float *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
-        for (int l = 0; l < lmax; ++l) {
-            const int nblocks = (l + 1 + MBLK - 1) / MBLK;
-            const int mblk = (((l + 1 + nblocks - 1) / nblocks) + 3) & ~3;  // balanced, multiple of 4
-            const int nslabs = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->sm_count / nblocks, ntiles));
-            const int tpc = (int)((ntiles + nslabs - 1) / nslabs);
+    for (auto &gr : groups) {
+        const int c0 = gr.first, c1 = gr.second, gn = c1 - c0;
+        // workspace: per catalog records + rows; shared sort scratch sized for the largest
+        int64_t smax = 0;
+        size_t ws_bytes = 0;
+        std::vector<size_t> off_pts(gn), off_rows(gn);
+        for (int c = c0; c < c1; ++c) smax = std::max(smax, cats[c].stride);
+        const size_t keyb = al256((size_t)smax * 4), histb = al256((size_t)256 * ((smax + 4095) / 4096 + 1) * 4);
+        ws_bytes = 4 * keyb + histb;
+        for (int c = c0; c < c1; ++c) {
+            off_pts[c - c0] = ws_bytes;
+            ws_bytes += al256((size_t)cats[c].stride * sizeof(SplitPt));
+            off_rows[c - c0] = ws_bytes;
+            ws_bytes += al256((size_t)3 * cats[c].stride * cats[c].in.lmax * sizeof(float));
+        }
+        CG_CUDA_TRY(ctx->split_ws.ensure(ws_bytes));
+        char *ws = ctx->split_ws.as<char>();
+        uint32_t *keys = reinterpret_cast<uint32_t *>(ws), *perm = reinterpret_cast<uint32_t *>(ws + keyb);
+        uint32_t *tk = reinterpret_cast<uint32_t *>(ws + 2 * keyb), *tv = reinterpret_cast<uint32_t *>(ws + 3 * keyb);
+        uint32_t *hist = reinterpret_cast<uint32_t *>(ws + 4 * keyb);
+        // ---- per catalog: radius sort and point records ----
+        for (int c = c0; c < c1; ++c) {
+            CatPlan &P = cats[c];
+            const int64_t n = P.in.n;
+            SplitPt *spts = reinterpret_cast<SplitPt *>(ws + off_pts[c - c0]);
+            k_split_keys<<<ceil_div(n, 256), 256, 0, st>>>(P.in.pts, n, P.max_r > 0.0 ? 1.0 / P.max_r : 0.0, keys,
+                                                           perm);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+            s = radix_sort_pairs(keys, perm, tk, tv, n, 16, hist, st);
+            if (s != CATANA_OK) return s;
+            const int64_t npad = P.ntiles * KT;
+            k_split_prep<<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts, P.in.w, perm, n, npad, spts, err_dev);
+            count_launch();
+            CG_CUDA_TRY(cudaGetLastError());
+        }
+        // ---- plan tables: catalogs, kz / jscale / nmax_l per catalog, items and reductions per level ----
+        int lmax_g = 0;
+        for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
+        std::vector<char> host;  // packed plan
+        auto put = [&host](const void *p, size_t b) {
+            const size_t o = al256(host.size());
+            host.resize(o + b);
+            memcpy(host.data() + o, p, b);
+            return o;
+        };
+        std::vector<size_t> o_kz(gn), o_js(gn), o_nl(gn);
+        for (int c = c0; c < c1; ++c) {
+            CatPlan &P = cats[c];
+            const int L = P.in.lmax, M = P.in.nmax;
+            std::vector<float2> kz((size_t)L * M);
+            for (size_t t = 0; t < kz.size(); ++t) {
+                float hi, lo;
+                split_ff(P.kh[t] / H, hi, lo);
+                kz[t] = make_float2(hi, lo);
+            }
+            std::vector<float> js(L);
+            for (int l = 0; l < L; ++l) {
+                const double mj = l < (int)ctx->split_cache.maxj.size() ? ctx->split_cache.maxj[l] : 1.0;
+                const int e = (int)std::floor(std::log2(32768.0 / (mj * P.max_w)));
+                js[l] = (float)std::ldexp(1.0, std::max(-60, std::min(100, e)));
+            }
+            o_kz[c - c0] = put(kz.data(), kz.size() * sizeof(float2));
+            o_js[c - c0] = put(js.data(), js.size() * sizeof(float));
+            o_nl[c - c0] = put(P.nmax_l.data(), P.nmax_l.size() * sizeof(int));
+        }
+        // catalog descriptors (fixed for the group)
+        const size_t o_cats = al256(host.size());
+        host.resize(o_cats + (size_t)gn * sizeof(SplitCat));
+        const size_t o_dyn = al256(host.size());  // items and reductions follow
+        for (int c = c0; c < c1; ++c) {
+            CatPlan &P = cats[c];
+            SplitCat sc;
+            sc.pts = reinterpret_cast<const SplitPt *>(ws + off_pts[c - c0]);
+            sc.rows = reinterpret_cast<float *>(ws + off_rows[c - c0]);
+            sc.n = P.in.n;
+            sc.stride = (int)P.stride;
+            sc.lrows = P.in.lmax;
+            sc.kzw = P.in.nmax;
+            sc.pad_ = 0;
+            sc.kz = nullptr;  // patched below, once the plan buffer's address is known
+            sc.jscale = nullptr;
+            sc.nmax_l = nullptr;
+            memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
+        }
+        // Work items of every level for a schedule of `waves` CTAs per SM: at level l
+        // the group's tiles x m-blocks are cut into slabs of T tiles, T chosen so the
+        // items fill about waves x SMs CTAs.  Items of one catalog are block-major.
+        struct Sched {
+            std::vector<SplitItem> items;
+            std::vector<SplitRed> reds;
+            std::vector<int> item0, red0, maxn;
+            std::vector<double> flops;
+        };
+        auto schedule = [&](double waves, Sched &S) {
+            S.items.clear();
+            S.reds.clear();
+            S.item0.assign(lmax_g + 1, 0);
+            S.red0.assign(lmax_g + 1, 0);
+            S.maxn.assign(lmax_g, 0);
+            S.flops.assign(lmax_g, 0.0);
+            for (int l = 0; l < lmax_g; ++l) {
+                S.item0[l] = (int)S.items.size();
+                S.red0[l] = (int)S.reds.size();
+                const int nblocks = (l + 1 + MBLK - 1) / MBLK;
+                const int mblk = (((l + 1 + nblocks - 1) / nblocks) + 3) & ~3;  // balanced, multiple of 4
+                // the active catalogs, largest first: the CTAs of a launch start
+                // roughly in index order, so the long items start first
+                std::vector<int> act;
+                int64_t tmax = 1;
+                for (int c = c0; c < c1; ++c)
+                    if (l < cats[c].in.lmax && cats[c].nmax_l[l] > 0) {
+                        act.push_back(c);
+                        tmax = std::max(tmax, cats[c].ntiles);
+                    }
+                std::stable_sort(act.begin(), act.end(),
+                                 [&](int x, int y) { return cats[x].ntiles > cats[y].ntiles; });
+                // slab length T: the largest for which the level still has at least
+                // waves x SMs items (small catalogs contribute one short item each)
+                const double slots = std::max(1.0, waves * ctx->sm_count);
+                auto nitems = [&](int64_t T) {
+                    double k = 0.0;
+                    for (int c : act) k += (double)nblocks * (double)((cats[c].ntiles + T - 1) / T);
+                    return k;
+                };
+                int64_t T = 1;
+                if (nitems(1) > slots) {
+                    int64_t lo = 1, hi = tmax;  // nitems(lo) >= slots
+                    while (lo < hi) {
+                        const int64_t mid = lo + (hi - lo + 1) / 2;
+                        if (nitems(mid) >= slots) lo = mid; else hi = mid - 1;
+                    }
+                    T = lo;
+                }
+                for (int c : act) {
+                    CatPlan &P = cats[c];
+                    const int nslabs = (int)((P.ntiles + T - 1) / T);
+                    const int64_t Tc = (P.ntiles + nslabs - 1) / nslabs;  // even slabs within the catalog
+                    SplitRed r;
+                    r.item0 = (int)(S.items.size() - S.item0[l]);
+                    r.nslabs = nslabs;
+                    r.mblk = mblk;
+                    r.nmax_l = P.nmax_l[l];
+                    r.kzw = P.in.nmax;
+                    r.pad_ = 0;
+                    r.fl = reinterpret_cast<double2 *>(P.in.f_acc) + (size_t)P.in.nmax * l * (l + 1) / 2;
+                    r.kln_row = P.in.kln_dev + (size_t)l * P.in.nmax;
+                    S.reds.push_back(r);
+                    S.maxn[l] = std::max(S.maxn[l], P.nmax_l[l]);
+                    S.flops[l] += 4.0 * (double)P.in.n * P.nmax_l[l] * (l + 1);
+                    for (int bk = 0; bk < nblocks; ++bk) {
+                        const int mb0 = bk * mblk;
+                        for (int sl = 0; sl < nslabs; ++sl) {
+                            SplitItem it;
+                            it.cat = c - c0;
+                            it.mb0 = mb0;
+                            it.mcount = std::min(mblk, l + 1 - mb0);
+                            it.pad_ = 0;
+                            it.t0 = (int64_t)sl * Tc;
+                            it.t1 = std::min<int64_t>(P.ntiles, it.t0 + Tc);
+                            S.items.push_back(it);
+                        }
+                    }
+                }
+            }
+            S.item0[lmax_g] = (int)S.items.size();
+            S.red0[lmax_g] = (int)S.reds.size();
+        };
+        // upload: [catalog tables | catalog descriptors | items | reductions]
+        char *pd = nullptr;
+        size_t o_items = 0, o_reds = 0;
+        auto upload = [&](const Sched &S) -> catana_status_t {
+            const size_t ib = S.items.size() * sizeof(SplitItem), rb = S.reds.size() * sizeof(SplitRed);
+            o_items = o_dyn;
+            o_reds = al256(o_items + ib);
+            const size_t total = o_reds + rb + 256;
+            CG_CUDA_TRY(ctx->split_plan.ensure(total));
+            pd = ctx->split_plan.as<char>();
+            host.resize(std::max(host.size(), total));
+            for (int c = c0; c < c1; ++c) {
+                SplitCat *sc = reinterpret_cast<SplitCat *>(host.data() + o_cats) + (c - c0);
+                sc->kz = reinterpret_cast<const float2 *>(pd + o_kz[c - c0]);
+                sc->jscale = reinterpret_cast<const float *>(pd + o_js[c - c0]);
+                sc->nmax_l = reinterpret_cast<const int *>(pd + o_nl[c - c0]);
+            }
+            if (ib) memcpy(host.data() + o_items, S.items.data(), ib);
+            if (rb) memcpy(host.data() + o_reds, S.reds.data(), rb);
+            CG_CUDA_TRY(cudaMemcpyAsync(pd, host.data(), o_reds + rb, cudaMemcpyHostToDevice, st));
+            int max_items = 1;
+            for (int l = 0; l < lmax_g; ++l) max_items = std::max(max_items, S.item0[l + 1] - S.item0[l]);
+            CG_CUDA_TRY(ctx->partial.ensure((size_t)max_items * 256 * 128 * sizeof(float)));
+            return CATANA_OK;
+        };
+        auto level_args = [&](const Sched &S, int l) {
             SplitArgs a;
             a.l = l;
-            a.nmax = nmax;
-            a.nint = nint;
-            a.nblocks = nblocks;
-            a.mblk = mblk;
-            a.n = nc;
-            a.stride = (int)stride;
-            a.tiles_per_cta = tpc;
-            a.pts = spts;
-            a.st1 = st1;
-            a.st2 = st2;
-            a.st0 = st0;
+            a.nint = nint_tab;
+            a.items = reinterpret_cast<const SplitItem *>(pd + o_items) + S.item0[l];
+            a.cats = reinterpret_cast<const SplitCat *>(pd + o_cats);
             a.coef = coef_d + (size_t)l * (l + 1) / 2;
-            a.kz = kz_d + (size_t)l * nmax;
-            a.tab = tab + (size_t)l * nint * 2;
-            a.jscale = jscale[l];
-            a.inv_scale = 1.0f / (jscale[l] * Y_SCALE);
-            a.partial = partial;
+            a.tab = tab + (size_t)l * nint_tab * 2;
+            a.partial = ctx->partial.as<float>();
             a.err = err_dev;
-            prof_begin(st);
-            k_split_l<<<dim3(nslabs, nblocks), NTHR, SMEM_BYTES, st>>>(a);
-            prof_end(st, 4.0 * (double)nc * nmax * (l + 1));
-            count_launch();
-            CG_CUDA_TRY(cudaGetLastError());
-            const int cnt = (l + 1) * nmax;
-            double2 *fl = reinterpret_cast<double2 *>(f_acc_dev) + (size_t)nmax * l * (l + 1) / 2;
-            k_split_reduce<<<ceil_div(cnt, 128), 128, 0, st>>>(partial, nslabs, nblocks, mblk, l + 1, nmax,
-                                                              kln_dev + (size_t)l * nmax, fl);
-            count_launch();
-            CG_CUDA_TRY(cudaGetLastError());
-            float *t = st2;
-            st2 = st1;
-            st1 = st0;
-            st0 = t;
+            return a;
+        };
+
+        double waves_use = waves;
+        if (waves_use <= 0.0) {
+            // autotune: time the contraction at three sample levels for each schedule
+            // (the rows those launches write are rewritten by the real level loop)
+            const std::string key = tune_key(cats, c0, c1);
+            auto hit = ctx->split_tuned.find(key);
+            if (hit != ctx->split_tuned.end()) {
+                waves_use = hit->second;
+            } else {
+                const double cand[] = {1.0, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0};
+                const int ls[3] = {std::max(1, lmax_g / 4), std::max(1, lmax_g / 2), std::max(1, (3 * lmax_g) / 4)};
+                cudaEvent_t e0, e1;
+                CG_CUDA_TRY(cudaEventCreate(&e0));
+                CG_CUDA_TRY(cudaEventCreate(&e1));
+                double best = 1e300;
+                waves_use = 1.0;
+                Sched S;
+                for (int rep = 0; rep < 2; ++rep)
+                    for (double w : cand) {
+                        schedule(w, S);
+                        s = upload(S);
+                        if (s != CATANA_OK) return s;
+                        CG_CUDA_TRY(cudaEventRecord(e0, st));
+                        for (int l : ls) {
+                            if (l >= lmax_g) continue;
+                            const int ni = S.item0[l + 1] - S.item0[l];
+                            if (ni == 0) continue;
+                            k_split_l<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
+                            count_launch();
+                        }
+                        CG_CUDA_TRY(cudaGetLastError());
+                        CG_CUDA_TRY(cudaEventRecord(e1, st));
+                        CG_CUDA_TRY(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        CG_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                        if (rep == 1 && ms < best) {
+                            best = ms;
+                            waves_use = w;
+                        }
+                    }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                ctx->split_tuned[key] = waves_use;
+            }
         }
+        ctx->split_last_waves = waves_use;
+        Sched S;
+        schedule(waves_use, S);
+        s = upload(S);
+        if (s != CATANA_OK) return s;
+        float *partial = ctx->partial.as<float>();
+        // ---- the level loop (optionally captured as one CUDA graph) ----
+        auto levels = [&](bool profile, cudaStream_t ls_st) -> catana_status_t {
+            for (int l = 0; l < lmax_g; ++l) {
+                const int ni = S.item0[l + 1] - S.item0[l];
+                const int nr = S.red0[l + 1] - S.red0[l];
+                if (ni == 0) continue;
+                if (profile) prof_begin(ls_st);
+                k_split_l<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
+                if (profile) prof_end(ls_st, S.flops[l]);
+                dim3 rg(ceil_div((int64_t)(l + 1) * S.maxn[l], 128), nr);
+                k_split_reduce<<<rg, 128, 0, ls_st>>>(partial, l + 1,
+                                                   reinterpret_cast<const SplitRed *>(pd + o_reds) + S.red0[l]);
+                count_launch(2);
+                CG_CUDA_TRY(cudaGetLastError());
+            }
+            return CATANA_OK;
+        };
+        if (use_graph) {
+            // captured on the context's own stream (the caller's may be the legacy
+            // default stream, which cannot capture) and launched on the caller's
+            if (!ctx->capture_stream)
+                CG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking));
+            cudaGraph_t graph = nullptr;
+            CG_CUDA_TRY(cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal));
+            catana_status_t ls = levels(false, ctx->capture_stream);
+            cudaError_t ce = cudaStreamEndCapture(ctx->capture_stream, &graph);
+            if (ls != CATANA_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return ls;
+            }
+            CG_CUDA_TRY(ce);
+            cudaGraphExec_t exec = nullptr;
+            cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            CG_CUDA_TRY(ie);
+            cudaError_t le = cudaGraphLaunch(exec, st);
+            cudaGraphExecDestroy(exec);
+            CG_CUDA_TRY(le);
+        } else {
+            s = levels(true, st);
+            if (s != CATANA_OK) return s;
+        }
+        // the next group reuses the workspace: finish this one first
+        if (groups.size() > 1) CG_CUDA_TRY(cudaStreamSynchronize(st));
     }
     return CATANA_OK;
+}
+
+catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
+                                     int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
+                                     double *f_acc_dev, int *err_dev, cudaStream_t st) {
+    if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
+    // chunks whose Legendre rows stay under 16 GB; they share the accumulator, so
+    // split_run places each in its own group and runs the groups one after another
+    const int64_t chunk = std::max<int64_t>(KT, std::min<int64_t>(npoints, (int64_t)(16e9 / (12.0 * lmax))));
+    std::vector<SplitCatInput> v;
+    for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
+        SplitCatInput in;
+        in.pts = points_dev + 3 * c0;
+        in.w = weights_dev ? weights_dev + c0 : nullptr;
+        in.n = std::min(chunk, npoints - c0);
+        in.lmax = lmax;
+        in.nmax = nmax;
+        in.rmax = rmax;
+        in.kmax = 0.0;
+        in.kln_dev = const_cast<double *>(kln_dev);
+        in.f_acc = f_acc_dev;
+        v.push_back(in);
+    }
+    return split_run(ctx, v, false, 1.0, err_dev, st);
 }
 
 }  // namespace catana_gpu

@@ -16,6 +16,7 @@ Keyword extensions (absent in the reference, defaults reproduce it):
   conj_fix=False       HEALPix only: conjugate aliased ring coefficients instead of
                        reproducing the reference's unconjugated read.
 """
+import ctypes
 import sys
 import time
 
@@ -153,6 +154,66 @@ def sfb_decomposition_healpix(pixelized_point_container, lmax, nmax, rmax, store
         raise TypeError("sfb_decomposition_healpix expects a PixelizedPointContainer")
     return sfb_decomposition(pixelized_point_container, lmax, nmax, rmax, store_flmn, verbose,
                              interpolation=interpolation, conj_fix=conj_fix)
+
+
+def sfb_decomposition_batched(point_containers, lmax, nmax, rmax, kmax=None, weights=None, store_flmn=False,
+                              verbose=True, precision="split", interpolation="auto", waves=0.0, graph=True):
+    """Decompose many catalogs in one call (no counterpart in the reference).
+
+    point_containers: sequence of PointContainer (or (N, 3) arrays of r, theta, phi).
+    lmax, nmax, rmax, kmax, weights: one value for all catalogs or one per catalog;
+    kmax > 0 keeps only the modes with k_ln <= kmax (the others have f = C = 0).
+    precision='split' runs all catalogs level by level in grouped tcgen05 launches,
+    captured as one CUDA graph (graph=False launches the levels directly); waves <= 0
+    autotunes the work-item size.  precision='plain' runs the FP64 path per catalog.
+    Returns a list of KClkk.
+    """
+    cats = list(point_containers)
+    nc = len(cats)
+
+    def per(v, name, conv):
+        if isinstance(v, (list, tuple, np.ndarray)):
+            if len(v) != nc:
+                raise ValueError("%s: one value per catalog expected" % name)
+            return [conv(x) for x in v]
+        return [conv(v)] * nc
+
+    lmaxs = per(lmax, "lmax", lambda x: _unsigned_short(x, "lmax"))
+    nmaxs = per(nmax, "nmax", lambda x: _unsigned_short(x, "nmax"))
+    rmaxs = per(rmax, "rmax", float)
+    kmaxs = per(0.0 if kmax is None else kmax, "kmax", lambda x: 0.0 if x is None else float(x))
+    ws = [None] * nc if weights is None else per(weights, "weights", lambda x: x)
+    flags = _flags(interpolation, precision) | (0 if graph else _lib.BATCH_NO_GRAPH)
+    recs = (_lib.Catalog * max(nc, 1))()
+    keep, out = [], []
+    for i, pc in enumerate(cats):
+        pts = np.ascontiguousarray(np.asarray(pc, dtype=np.float64).reshape(-1, 3))
+        w = None
+        if ws[i] is not None:
+            w = np.ascontiguousarray(ws[i], dtype=np.float64).reshape(-1)
+            if w.shape[0] != pts.shape[0]:
+                raise ValueError("weights of catalog %d must have one entry per point" % i)
+        k = np.zeros((lmaxs[i], nmaxs[i]))
+        c = np.zeros((lmaxs[i], nmaxs[i]))
+        f = np.zeros(int(_lib.lib.catana_gpu_flmn_size(lmaxs[i], nmaxs[i])), dtype=np.complex128) \
+            if store_flmn else None
+        r = recs[i]
+        r.points, r.weights, r.npoints = pts.ctypes.data, (w.ctypes.data if w is not None else None), pts.shape[0]
+        r.rmax, r.kmax, r.lmax, r.nmax = rmaxs[i], kmaxs[i], lmaxs[i], nmaxs[i]
+        r.k_ln, r.c_ln, r.f_lmn = k.ctypes.data, c.ctypes.data, (f.ctypes.data if f is not None else None)
+        keep.append((pts, w))
+        out.append((k, c, f))
+    if verbose:
+        print("SFB decomposition (raw method, batched): %d catalogs, %d points" %
+              (nc, sum(p.shape[0] for p, _ in keep)))
+        sys.stdout.flush()
+    t0 = time.perf_counter()
+    st = _lib.lib.catana_gpu_sfb_raw_batched(ctypes.cast(recs, ctypes.c_void_p), nc, flags, float(waves), None)
+    _lib.check(st, "sfb_raw_batched")
+    if verbose:
+        print("Done (%.3f s)." % (time.perf_counter() - t0))
+    return [KClkk(k, c, unpack_flmn(f, lmaxs[i], nmaxs[i]) if store_flmn else [])
+            for i, (k, c, f) in enumerate(out)]
 
 
 def compute_kln(lmax, nmax, rmax):

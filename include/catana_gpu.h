@@ -118,6 +118,49 @@ catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, const doubl
                                            double *k_ln_dev, double *c_ln_dev, double *f_lmn_dev,
                                            catana_gpu_stream_t stream);
 
+/* ---- batched raw decomposition (no counterpart in the reference) ---------
+ * Many catalogs, each with its own size, lmax, nmax, rmax and an optional kmax cut,
+ * decomposed in one call.  Each catalog's outputs are those of catana_gpu_sfb_raw
+ * on that catalog alone, except that with kmax > 0 the modes with k_ln > kmax are
+ * not computed: their f_lmn and c_ln are 0 (k_ln is still filled in full). */
+typedef struct {
+    const double *points;   /* npoints x 3 (r, theta, phi) */
+    const double *weights;  /* optional per-point weights (NULL = unit) */
+    int64_t npoints;
+    double rmax;
+    double kmax;            /* > 0: keep only modes with k_ln <= kmax */
+    double *k_ln;           /* lmax x nmax, row-major [l][n] */
+    double *c_ln;           /* lmax x nmax */
+    double *f_lmn;          /* packed as for catana_gpu_sfb_raw, or NULL */
+    uint16_t lmax, nmax;
+    uint32_t reserved;      /* 0 */
+} catana_catalog_t;
+
+/* Batched flags (combine with CATANA_FORM_* and, for the plain form, CATANA_JL_*). */
+#define CATANA_BATCH_NO_GRAPH 16u  /* split form: launch the level loop directly
+                                      instead of capturing it as one CUDA graph */
+
+/* Split form: the catalogs advance level by level together -- at each l one
+ * grouped tcgen05 launch covers every catalog's (m-block, tile-slab) work items and
+ * one grouped reduction folds them into each catalog's f -- and the whole level
+ * loop is captured and launched as one CUDA graph.  `waves` sets how many CTAs per
+ * SM each level's items are cut for; waves <= 0 autotunes it (times the
+ * contraction at three sample levels for several schedules, once per distinct
+ * catalog set; catana_gpu_batch_waves() reports the choice).  Plain form: the
+ * catalogs run one after another through the FP64 path (waves ignored).
+ * Host pointers in the catalog records; blocks until the results are in place. */
+catana_status_t catana_gpu_sfb_raw_batched(const catana_catalog_t *cats, int32_t ncat, uint32_t flags, double waves,
+                                           catana_gpu_stream_t stream);
+
+/* The same with device pointers in the catalog records (the record array itself
+ * stays on the host); enqueued on `stream`.  It synchronises once to read the
+ * catalogs' extents and weight sums.  *status_dev as for catana_gpu_sfb_raw_dev. */
+catana_status_t catana_gpu_sfb_raw_batched_dev(const catana_catalog_t *cats, int32_t ncat, uint32_t flags,
+                                               double waves, int *status_dev, catana_gpu_stream_t stream);
+
+/* Waves per SM the last split-form run used (the autotuned value when it tuned). */
+double catana_gpu_batch_waves(void);
+
 /* HEALPix (pixelized) SFB decomposition.  The catalog is given binned: pixel p
  * (RING scheme) holds the radii r_sorted[pix_offsets[p] .. pix_offsets[p+1]), in
  * the order the points were added.  npix = 12 nside^2; pix_offsets has npix+1

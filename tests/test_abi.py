@@ -123,3 +123,19 @@ def test_savetxt_format(tmp_path):
     assert np.array_equal(np.loadtxt(base + ".c_ln", ndmin=2), c)
     with pytest.raises(ValueError):
         r.k_ln[0, 0] = 1.0
+
+
+def test_batched_argument_validation():
+    """The batched entry point rejects bad records before it touches a device."""
+    pc = catana.PointContainer(np.ones((3, 3)))
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc, pc], 4, 4, 10.0, kmax=-1.0, verbose=False)
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc, pc], 4, 4, [10.0, 0.0], verbose=False)
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc, pc], [4], 4, 10.0, verbose=False)
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc], 4, 4, 10.0, weights=[np.ones(2)], verbose=False)
+    assert _lib.lib.catana_gpu_sfb_raw_batched(None, -1, 0, 0.0, None) == _lib.ERR_ARG
+    assert _lib.lib.catana_gpu_sfb_raw_batched(None, 0, 0, 0.0, None) == _lib.OK
+    assert ctypes.sizeof(_lib.Catalog) == 72
