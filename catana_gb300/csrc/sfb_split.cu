@@ -8,8 +8,10 @@
 // Jlo*Yhi).  Both operands are scaled by powers of two towards the top of the FP16
 // range so the lo halves stay normal.
 //
-// Work split: one launch per l; a CTA owns one block of <= 128 complex m (so l >= 128
-// uses two CTAs per slab, each generating the J tile) and a slab of 32-point tiles.
+// Work split: one launch per l; a CTA owns one work item: a catalog, a block of <= 128
+// complex m (so l >= 128 uses two items per slab, each generating the J tile), a half
+// of <= 128 radial orders (nmax > 128 uses two, each generating the Y tile; the first
+// writes the Legendre rows) and a slab of 32-point tiles.
 // Accumulation: the tensor core accumulates one tile (6 MMAs) into D_tile in tensor
 // memory; the CTA then folds D_tile into a second tensor-memory region D_acc with
 // FP32 round-to-nearest adds on the CUDA cores (the tensor core's own FP32
@@ -18,9 +20,10 @@
 // partials in FP64 in fixed order and applies k_ln.
 //
 // Operand generation (CUDA cores, FP32 with float-float inputs):
-//   * j_l from a per-l piecewise degree-5 polynomial on intervals of width 1/2 in
-//     z = k r (Chebyshev interpolation of the FP64 j_l; error <= 1.2e-7 of the
-//     envelope including the FP32 coefficients), the argument formed as a float-float
+//   * j_l from a per-l piecewise degree-6 polynomial on unit intervals of z = k r
+//     centred on the integers (Chebyshev interpolation of the FP64 j_l, monomial
+//     coefficients in u = z - round(z) in [-1/2, 1/2]; error <= ~1e-7 of the envelope,
+//     dominated by the FP32 coefficients), the argument formed as a float-float
 //     product so its absolute error is ~1e-12;
 //   * P_lm by one step of the l-recurrence from FP32 rows P_{l-1}, P_{l-2} in HBM
 //     (staged into shared memory one tile ahead with cp.async), with the recurrence
@@ -57,9 +60,11 @@ constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator 
 constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
 constexpr int FLUSH_FOLDS = 32;     // folds into the TMEM sum before it goes to global memory
 constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
-constexpr double H = 0.5;           // table interval width in z
+constexpr double H = 1.0;           // table interval width in z (intervals centred on integers)
+constexpr int TDEG = 6;             // table polynomial degree (7 coefficients in two float4)
 constexpr int SPLIT_LMAX = 256;     // scaled-row range limit (see header comment)
-constexpr int SPLIT_NMAX = 128;     // one 128-lane accumulator tile
+constexpr int SPLIT_NMAX = 256;     // two 128-lane halves (separate work items)
+constexpr int NHALF = 128;          // radial orders per work item (accumulator lanes)
 constexpr uint64_t WAIT_NS = 1000000000ull;
 
 // shared-memory map (bytes, from a 1024-aligned base)
@@ -73,7 +78,7 @@ constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS; // P_{l-1}, P_{l-2} and t
 constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
 constexpr uint32_t SM_TAB = NINT_MAX * 32;
 constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;
-constexpr uint32_t OFF_COEF = OFF_KZ + SPLIT_NMAX * 8;
+constexpr uint32_t OFF_COEF = OFF_KZ + NHALF * 8;
 constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
@@ -108,7 +113,7 @@ struct SplitCat {
 
 // One CTA of a level launch: a catalog, a block of complex m, a range of tiles.
 struct SplitItem {
-    int cat, mb0, mcount, pad_;
+    int cat, mb0, mcount, n0;  // n0: first radial order of the item's 128-lane half
     int64_t t0, t1;
 };
 
@@ -158,7 +163,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const SplitCat cat = a.cats[item.cat];
     const int mb0 = item.mb0;
     const int mcount = item.mcount;
-    const int nmax = cat.nmax_l[l];
+    const int nh0 = item.n0;
+    const int nmax = min(NHALF, cat.nmax_l[l] - nh0);  // radial orders of this half
+    const bool wrows = (nh0 == 0);                      // the first half writes the Legendre rows
     const float jscale = cat.jscale[l];
     const float inv_scale = 1.0f / (jscale * Y_SCALE);
     const int ncols = 2 * mcount;
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
     float2 *s_kz = reinterpret_cast<float2 *>(sm + OFF_KZ);
     float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);
-    const float2 *kz_row = cat.kz + (size_t)l * cat.kzw;
+    const float2 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
     for (int t = tid; t < nmax; t += NTHR) s_kz[t] = kz_row[t];
     for (int t = tid; t < mcount; t += NTHR) s_coef[t] = a.coef[mb0 + t];
@@ -324,15 +331,16 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                     float e = fmaf(rh, kk.x, -p);
                     e = fmaf(rh, kk.y, e);
                     e = fmaf(rl, kk.x, e);
-                    const float fl = floorf(p);
+                    const float fl = rintf(p);
                     int idx = (int)fl;
-                    const float uu = (p - fl) + e;
+                    const float uu = (p - fl) + e;  // in [-1/2, 1/2]
                     if ((unsigned)idx >= (unsigned)a.nint) {
                         *a.err = CATANA_ERR_DOMAIN;
                         idx = idx < 0 ? 0 : a.nint - 1;
                     }
                     const float4 c0 = s_tab[2 * idx], c1 = s_tab[2 * idx + 1];
-                    float jv = fmaf(c1.y, uu, c1.x);
+                    float jv = fmaf(c1.z, uu, c1.y);
+                    jv = fmaf(jv, uu, c1.x);
                     jv = fmaf(jv, uu, c0.w);
                     jv = fmaf(jv, uu, c0.z);
                     jv = fmaf(jv, uu, c0.y);
@@ -383,7 +391,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                                 const float vv = fmaf(c.y, tt, -bb);
                                 P = fmaf(c.x, tt, vv);
                             }
-                            st0[(int64_t)m * stride + i] = P;
+                            if (wrows) st0[(int64_t)m * stride + i] = P;
                             const float Pu = P * Y_UNSCALE;
                             yr = Pu * cm;
                             yi = -Pu * smv;
@@ -464,7 +472,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
 
 // One catalog's reduction at one level: its items are ordered block-major, then slab.
 struct SplitRed {
-    int item0, nslabs, mblk, nmax_l, kzw, pad_;
+    int item0, nslabs, mblk, nmax_l, kzw, nhalves;  // items: block-major, then half, then slab
     double2 *fl;            // f accumulator block of l: [m][kzw]
     const double *kln_row;  // k_ln row l (kzw entries)
 };
@@ -477,11 +485,12 @@ __global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const
     if (t >= lp1 * r.nmax_l) return;
     const int m = t / r.nmax_l, n = t - m * r.nmax_l;
     const int blk = m / r.mblk, ml = m - blk * r.mblk;
+    const int hf = n / NHALF, nl = n - hf * NHALF;
     double sr = 0.0, si = 0.0;
     for (int sl = 0; sl < r.nslabs; ++sl) {
-        const float *p = partial + (size_t)(r.item0 + blk * r.nslabs + sl) * 256 * 128;
-        sr += (double)p[(size_t)(2 * ml) * 128 + n];
-        si += (double)p[(size_t)(2 * ml + 1) * 128 + n];
+        const float *p = partial + (size_t)(r.item0 + (blk * r.nhalves + hf) * r.nslabs + sl) * 256 * 128;
+        sr += (double)p[(size_t)(2 * ml) * 128 + nl];
+        si += (double)p[(size_t)(2 * ml + 1) * 128 + nl];
     }
     const double k = r.kln_row[n];
     double2 *o = r.fl + (size_t)m * r.kzw + n;
@@ -561,33 +570,37 @@ __global__ void k_split_maxes(const double *__restrict__ pts, const double *__re
 }
 
 // j_l at the 6 Chebyshev nodes of every interval, all l at once per node (FP64).
+// Chebyshev node k of the degree-TDEG interpolant on an interval, as an offset in [-1/2, 1/2]
+__host__ __device__ inline double cheb_node(int k) { return 0.5 * cos((2.0 * k + 1.0) * kPi / (2.0 * (TDEG + 1))); }
+
 __global__ void k_split_nodes(int lmax, int nint, double *vals /* [node][lmax] */) {
     const int node = blockIdx.x * blockDim.x + threadIdx.x;
-    if (node >= nint * 6) return;
-    const int j = node / 6, k = node - 6 * j;
-    const double tk = 0.5 - 0.5 * cos((2.0 * k + 1.0) * kPi / 12.0);  // Chebyshev node in [0, 1]
-    const double z = H * (j + tk);
+    if (node >= nint * (TDEG + 1)) return;
+    const int j = node / (TDEG + 1), k = node - (TDEG + 1) * j;
+    const double z = H * (j + cheb_node(k));  // interval j is centred on z = j H
     double buf[SPLIT_LMAX + 1];
-    sbessel_jl_all(lmax, z, buf);
-    for (int l = 0; l < lmax; ++l) vals[(size_t)node * lmax + l] = buf[l];
+    sbessel_jl_all(lmax, fabs(z), buf);
+    for (int l = 0; l < lmax; ++l)  // j_l(-z) = (-1)^l j_l(z): the first interval straddles 0
+        vals[(size_t)node * lmax + l] = (z < 0.0 && (l & 1)) ? -buf[l] : buf[l];
 }
 
-// monomial coefficients in u in [0,1] of the interpolant through the 6 nodes
-__global__ void k_split_coefs(int lmax, int nint, const double *vals, const double *vinv /* 6x6 */,
+// monomial coefficients in u in [-1/2, 1/2] of the interpolant through the nodes
+__global__ void k_split_coefs(int lmax, int nint, const double *vals, const double *vinv,
                               float4 *tab /* [l][nint][2] */) {
+    constexpr int NC = TDEG + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= lmax * nint) return;
     const int l = t / nint, j = t - l * nint;
-    double y[6], c[6];
-    for (int k = 0; k < 6; ++k) y[k] = vals[(size_t)(6 * j + k) * lmax + l];
-    for (int r = 0; r < 6; ++r) {
+    double y[NC], c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < NC; ++k) y[k] = vals[(size_t)(NC * j + k) * lmax + l];
+    for (int r = 0; r < NC; ++r) {
         double s = 0.0;
-        for (int k = 0; k < 6; ++k) s += vinv[6 * r + k] * y[k];
+        for (int k = 0; k < NC; ++k) s += vinv[NC * r + k] * y[k];
         c[r] = s;
     }
     float4 *o = tab + ((size_t)l * nint + j) * 2;
     o[0] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
-    o[1] = make_float4((float)c[4], (float)c[5], 0.f, 0.f);
+    o[1] = make_float4((float)c[4], (float)c[5], (float)c[6], (float)c[7]);
 }
 
 void split_ff(double v, float &hi, float &lo) {
@@ -595,35 +608,36 @@ void split_ff(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
-// inverse of the 6x6 Vandermonde matrix at the Chebyshev nodes (FP64, Gauss-Jordan)
+// inverse of the Vandermonde matrix V[k][r] = u_k^r at the Chebyshev nodes (FP64,
+// Gauss-Jordan with partial pivoting), row-major NC x NC
 std::vector<double> cheb_vandermonde_inverse() {
-    double A[6][12];
-    for (int k = 0; k < 6; ++k) {
-        const double tk = 0.5 - 0.5 * std::cos((2.0 * k + 1.0) * kPi / 12.0);
+    constexpr int NC = TDEG + 1;
+    double A[NC][2 * NC];
+    for (int k = 0; k < NC; ++k) {
+        const double tk = cheb_node(k);
         double p = 1.0;
-        for (int r = 0; r < 6; ++r) {
+        for (int r = 0; r < NC; ++r) {
             A[k][r] = p;
             p *= tk;
         }
-        for (int r = 0; r < 6; ++r) A[k][6 + r] = (r == k) ? 1.0 : 0.0;
+        for (int r = 0; r < NC; ++r) A[k][NC + r] = (r == k) ? 1.0 : 0.0;
     }
-    for (int col = 0; col < 6; ++col) {
+    for (int col = 0; col < NC; ++col) {
         int piv = col;
-        for (int r = col + 1; r < 6; ++r)
+        for (int r = col + 1; r < NC; ++r)
             if (std::fabs(A[r][col]) > std::fabs(A[piv][col])) piv = r;
-        for (int c = 0; c < 12; ++c) std::swap(A[col][c], A[piv][c]);
+        for (int c = 0; c < 2 * NC; ++c) std::swap(A[col][c], A[piv][c]);
         const double d = A[col][col];
-        for (int c = 0; c < 12; ++c) A[col][c] /= d;
-        for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 2 * NC; ++c) A[col][c] /= d;
+        for (int r = 0; r < NC; ++r)
             if (r != col) {
                 const double f = A[r][col];
-                for (int c = 0; c < 12; ++c) A[r][c] -= f * A[col][c];
+                for (int c = 0; c < 2 * NC; ++c) A[r][c] -= f * A[col][c];
             }
     }
-    // A[:, 6:] = V^{-1} with V[k][r] = t_k^r, so c = V^{-1} y
-    std::vector<double> inv(36);
-    for (int r = 0; r < 6; ++r)
-        for (int k = 0; k < 6; ++k) inv[6 * r + k] = A[r][6 + k];
+    std::vector<double> inv(NC * NC);
+    for (int r = 0; r < NC; ++r)
+        for (int k = 0; k < NC; ++k) inv[NC * r + k] = A[r][NC + k];
     return inv;
 }
 
@@ -653,14 +667,15 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
     const size_t tab_bytes = (size_t)lmax * nint * 2 * sizeof(float4);
     const size_t coef_bytes = (size_t)lmax * (lmax + 1) / 2 * sizeof(float4);
     CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + coef_bytes + 1024));
-    const size_t vbytes = (size_t)nint * 6 * lmax * sizeof(double);
+    constexpr int NC = TDEG + 1;
+    const size_t vbytes = (size_t)nint * NC * lmax * sizeof(double);
     DevBuf tmp;
-    CG_CUDA_TRY(tmp.ensure(vbytes + 36 * sizeof(double)));
+    CG_CUDA_TRY(tmp.ensure(vbytes + NC * NC * sizeof(double)));
     double *vals = tmp.as<double>();
-    double *vinv = vals + (size_t)nint * 6 * lmax;
+    double *vinv = vals + (size_t)nint * NC * lmax;
     std::vector<double> vi = cheb_vandermonde_inverse();
-    CG_CUDA_TRY(cudaMemcpyAsync(vinv, vi.data(), 36 * sizeof(double), cudaMemcpyHostToDevice, st));
-    k_split_nodes<<<ceil_div(nint * 6, 64), 64, 0, st>>>(lmax, nint, vals);
+    CG_CUDA_TRY(cudaMemcpyAsync(vinv, vi.data(), NC * NC * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_split_nodes<<<ceil_div(nint * NC, 64), 64, 0, st>>>(lmax, nint, vals);
     count_launch();
     CG_CUDA_TRY(cudaGetLastError());
     float4 *tab = ctx->split_tab.as<float4>();
@@ -725,7 +740,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     std::vector<CatPlan> cats;
     for (auto &c : cats_in) {
         if (c.lmax > SPLIT_LMAX || c.nmax > SPLIT_NMAX) {
-            set_error("the split form supports lmax <= 256 and nmax <= 128");
+            set_error("the split form supports lmax <= 256 and nmax <= 256");
             return CATANA_ERR_ARG;
         }
         if (c.n <= 0 || c.lmax == 0 || c.nmax == 0) continue;
@@ -936,7 +951,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const double slots = std::max(1.0, waves * ctx->sm_count);
                 auto nitems = [&](int64_t T) {
                     double k = 0.0;
-                    for (int c : act) k += (double)nblocks * (double)((cats[c].ntiles + T - 1) / T);
+                    for (int c : act)
+                        k += (double)nblocks * ((cats[c].nmax_l[l] + NHALF - 1) / NHALF) *
+                             (double)((cats[c].ntiles + T - 1) / T);
                     return k;
                 };
                 int64_t T = 1;
@@ -958,7 +975,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                     r.mblk = mblk;
                     r.nmax_l = P.nmax_l[l];
                     r.kzw = P.in.nmax;
-                    r.pad_ = 0;
+                    r.nhalves = (P.nmax_l[l] + NHALF - 1) / NHALF;
                     r.fl = reinterpret_cast<double2 *>(P.in.f_acc) + (size_t)P.in.nmax * l * (l + 1) / 2;
                     r.kln_row = P.in.kln_dev + (size_t)l * P.in.nmax;
                     S.reds.push_back(r);
@@ -966,16 +983,17 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                     S.flops[l] += 4.0 * (double)P.in.n * P.nmax_l[l] * (l + 1);
                     for (int bk = 0; bk < nblocks; ++bk) {
                         const int mb0 = bk * mblk;
-                        for (int sl = 0; sl < nslabs; ++sl) {
-                            SplitItem it;
-                            it.cat = c - c0;
-                            it.mb0 = mb0;
-                            it.mcount = std::min(mblk, l + 1 - mb0);
-                            it.pad_ = 0;
-                            it.t0 = (int64_t)sl * Tc;
-                            it.t1 = std::min<int64_t>(P.ntiles, it.t0 + Tc);
-                            S.items.push_back(it);
-                        }
+                        for (int hf = 0; hf < r.nhalves; ++hf)
+                            for (int sl = 0; sl < nslabs; ++sl) {
+                                SplitItem it;
+                                it.cat = c - c0;
+                                it.mb0 = mb0;
+                                it.mcount = std::min(mblk, l + 1 - mb0);
+                                it.n0 = hf * NHALF;
+                                it.t0 = (int64_t)sl * Tc;
+                                it.t1 = std::min<int64_t>(P.ntiles, it.t0 + Tc);
+                                S.items.push_back(it);
+                            }
                     }
                 }
             }

@@ -45,6 +45,7 @@ def _check(res, f, c, tag):
     (5000, 33, 20, True),
     (2000, 130, 64, False),   # l >= 128: two m-blocks per slab
     (20000, 40, 100, False),  # many tiles per CTA: folds and flushes
+    (3000, 24, 200, True),    # nmax > 128: two radial halves
 ])
 def test_split_vs_oracle(sm103, n, lmax, nmax, weighted):
     pts = uniform_ball(n, 1000.0, seed=100 + n)
