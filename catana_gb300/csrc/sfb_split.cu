@@ -62,7 +62,8 @@ constexpr int FLUSH_FOLDS = 32;     // folds into the TMEM sum before it goes to
 constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
 constexpr double H = 1.0;           // table interval width in z (intervals centred on integers)
 constexpr int TDEG = 6;             // table polynomial degree (7 coefficients in two float4)
-constexpr int SPLIT_LMAX = 256;     // scaled-row range limit (see header comment)
+constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 (see header comment)
+constexpr int SPLIT_LMAX_EXT = 512; // with the 2-bit row exponents (extended range)
 constexpr int SPLIT_NMAX = 256;     // two 128-lane halves (separate work items)
 constexpr int NHALF = 128;          // radial orders per work item (accumulator lanes)
 constexpr uint64_t WAIT_NS = 1000000000ull;
@@ -74,7 +75,8 @@ constexpr uint32_t SM_BUF = 2 * SM_J + 2 * SM_Y;
 constexpr uint32_t OFF_ST = 2 * SM_BUF;                // staged Legendre rows, two stages
 constexpr uint32_t SM_STROW = MBLK * KT * 4;           // one row set (MBLK m x 32 points) = 16 KB
 constexpr uint32_t SM_STPTS = KT * 48;                 // the tile's 32 SplitPt records
-constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS; // P_{l-1}, P_{l-2} and the points
+constexpr uint32_t SM_STEXP = 2 * MBLK * 8;            // row exponent words of P_{l-1}, P_{l-2} (extended range)
+constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS + SM_STEXP;  // P_{l-1}, P_{l-2}, the points, exponents
 constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
 constexpr uint32_t SM_TAB = NINT_MAX * 32;
 constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;
@@ -105,7 +107,9 @@ struct SplitCat {
     int stride;             // row stride (multiple of 32, >= n)
     int lrows;              // rows per set (the catalog's lmax)
     int kzw;                // row width of kz (the catalog's nmax)
-    int pad_;
+    int epitch;             // exponent words per tile (lrows rounded up to even)
+    unsigned long long *rexp;  // extended range: three exponent sets [tile][lrows], set k at rexp + k * eset
+    int64_t eset;           // words per exponent set
     const float2 *kz;       // [l][kzw]: k_ln / H as float-float
     const float *jscale;    // [l]: 2^sJ
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
@@ -151,6 +155,11 @@ __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c
 
 // One CTA: multipole l, complex m in [128 b, 128 b + 128) of it (blockIdx.y = b),
 // a slab of 32-point tiles (blockIdx.x).
+// EXT: rows carry a 2-bit exponent per (point, m) -- the stored value is
+// P * 2^100 * 2^(128 e); e grows by one when a sectoral value drops below 2^-40 and
+// shrinks by one when a value grows past 2^40 along l, so seeds down to ~2^-520 stay
+// exact.  Values with e > 0 are below 2^-188 and enter Y as zero.
+template <bool EXT>
 __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -202,6 +211,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
     const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
     float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
+    const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
+    unsigned long long *ex0 = nullptr;
+    if (EXT) {
+        ex1 = cat.rexp + (size_t)((l + 2) % 3) * cat.eset;
+        ex2 = cat.rexp + (size_t)((l + 1) % 3) * cat.eset;
+        ex0 = cat.rexp + (size_t)(l % 3) * cat.eset;
+    }
     float *partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
@@ -230,6 +246,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             tc05::cp_async16(stg + 2 * SM_STROW + tid * 16,
                              reinterpret_cast<const uint8_t *>(cat.pts + i0) + tid * 16);
         if (l == 0) return;
+        if (EXT) {  // exponent words of the block's m (16-byte pieces; the sets carry a pad word)
+            const int ep = (mcount + 1) >> 1;
+            for (int c = tid; c < 2 * ep; c += NTHR) {
+                const int which = c >= ep;
+                const int pc = which ? c - ep : c;
+                const unsigned long long *src = (which ? ex2 : ex1) + t * cat.epitch + mb0 + 2 * pc;
+                tc05::cp_async16(stg + 2 * SM_STROW + SM_STPTS + which * MBLK * 8 + pc * 16, src);
+            }
+        }
         const int per_set = mcount * 8;  // 16-byte pieces per row set
         for (int c = tid; c < 2 * per_set; c += NTHR) {
             const int which = c >= per_set;
@@ -307,6 +332,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
         const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
         const float *stg2 = stg1 + MBLK * KT;
+        const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
+            sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE + 2 * SM_STROW + SM_STPTS);
+        const unsigned long long *stge2 = stge1 + MBLK;
         const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
                                                                 2 * SM_STROW + q * 48);
         const int64_t i = t * KT + q;
@@ -376,23 +404,58 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                         const int ml = ml0 + k;
                         const int m = mb0 + ml;
                         float yr = 0.f, yi = 0.f;
-                        if (ml < mhi && valid) {
-                            float P;
-                            if (l == 0) {
-                                P = P00_SCALED;
-                            } else {
-                                const float4 c = s_coef[ml];
-                                const float p1 = stg1[ml * KT + q];
-                                const bool sect = (m == l);
-                                const float xa = sect ? sh : xh, xb = sect ? sl : xl;
-                                const float tt = fmaf(xa, p1, xb * p1);
-                                const float p2 = (m <= l - 2) ? stg2[ml * KT + q] : 0.f;
-                                const float bb = fmaf(c.w, p2, c.z * p2);
-                                const float vv = fmaf(c.y, tt, -bb);
-                                P = fmaf(c.x, tt, vv);
+                        if (ml < mhi) {  // warp-uniform
+                            float P = 0.f;
+                            unsigned e = 0;
+                            if (valid) {
+                                if (l == 0) {
+                                    P = P00_SCALED;
+                                } else {
+                                    const float4 c = s_coef[ml];
+                                    float p1 = stg1[ml * KT + q];
+                                    const bool sect = (m == l);
+                                    const float xa = sect ? sh : xh, xb = sect ? sl : xl;
+                                    float p2 = (m <= l - 2) ? stg2[ml * KT + q] : 0.f;
+                                    if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
+                                        const unsigned long long w1 = stge1[sect ? ml - 1 : ml];
+                                        e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
+                                        if (m <= l - 2) {
+                                            const unsigned long long w2 = stge2[ml];
+                                            const unsigned e2 =
+                                                (unsigned)((w2 >> q) & 1ull) | ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
+                                            // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                            if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
+                                        }
+                                    }
+                                    const float tt = fmaf(xa, p1, xb * p1);
+                                    const float bb = fmaf(c.w, p2, c.z * p2);
+                                    const float vv = fmaf(c.y, tt, -bb);
+                                    P = fmaf(c.x, tt, vv);
+                                    if (EXT) {
+                                        const float ap = fabsf(P);
+                                        if (sect) {
+                                            if (ap < 0x1p-40f) {
+                                                if (e < 3) {
+                                                    P = P * 0x1p64f * 0x1p64f;
+                                                    ++e;
+                                                } else {
+                                                    P = 0.f;  // below 2^-520: no contribution within lmax
+                                                }
+                                            }
+                                        } else if (e > 0 && ap > 0x1p40f) {
+                                            P = P * 0x1p-64f * 0x1p-64f;
+                                            --e;
+                                        }
+                                    }
+                                }
+                                if (wrows) st0[(int64_t)m * stride + i] = P;
                             }
-                            if (wrows) st0[(int64_t)m * stride + i] = P;
-                            const float Pu = P * Y_UNSCALE;
+                            if (EXT && wrows) {
+                                const unsigned b0 = __ballot_sync(0xffffffffu, e & 1u);
+                                const unsigned b1 = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
+                                if (lane == 0) ex0[t * cat.epitch + m] = ((unsigned long long)b1 << 32) | b0;
+                            }
+                            const float Pu = (EXT && e != 0) ? 0.f : P * Y_UNSCALE;
                             yr = Pu * cm;
                             yi = -Pu * smv;
                         }
@@ -578,7 +641,7 @@ __global__ void k_split_nodes(int lmax, int nint, double *vals /* [node][lmax] *
     if (node >= nint * (TDEG + 1)) return;
     const int j = node / (TDEG + 1), k = node - (TDEG + 1) * j;
     const double z = H * (j + cheb_node(k));  // interval j is centred on z = j H
-    double buf[SPLIT_LMAX + 1];
+    double buf[SPLIT_LMAX_EXT + 1];
     sbessel_jl_all(lmax, fabs(z), buf);
     for (int l = 0; l < lmax; ++l)  // j_l(-z) = (-1)^l j_l(z): the first interval straddles 0
         vals[(size_t)node * lmax + l] = (z < 0.0 && (l & 1)) ? -buf[l] : buf[l];
@@ -721,6 +784,10 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
     return CATANA_OK;
 }
 
+// words of one exponent set: [tile][lmax rounded up to even] plus a pad word pair
+// (16-byte copies of an odd m count read one word past the block)
+int64_t exp_set_words(const CatPlan &P) { return P.ntiles * ((P.in.lmax + 1) & ~1) + 2; }
+
 // autotune cache key: catalog count, sizes and multipoles of a group
 std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
     std::string k = std::to_string(c1 - c0);
@@ -739,8 +806,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                           double waves, int *err_dev, cudaStream_t st) {
     std::vector<CatPlan> cats;
     for (auto &c : cats_in) {
-        if (c.lmax > SPLIT_LMAX || c.nmax > SPLIT_NMAX) {
-            set_error("the split form supports lmax <= 256 and nmax <= 256");
+        if (c.lmax > SPLIT_LMAX_EXT || c.nmax > SPLIT_NMAX) {
+            set_error("the split form supports lmax <= 512 and nmax <= 256");
             return CATANA_ERR_ARG;
         }
         if (c.n <= 0 || c.lmax == 0 || c.nmax == 0) continue;
@@ -755,7 +822,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     if (cats.empty()) return CATANA_OK;
     static bool attr = false;
     if (!attr) {
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
         attr = true;
     }
     // ---- extents: max r and max |w| per catalog (one synchronisation) ----
@@ -831,10 +899,14 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     }
     for (auto &gr : groups) {
         const int c0 = gr.first, c1 = gr.second, gn = c1 - c0;
-        // workspace: per catalog records + rows; shared sort scratch sized for the largest
+        int lmax_g = 0;
+        for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
+        const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
+        auto kern = ext ? k_split_l<true> : k_split_l<false>;
+        // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
         size_t ws_bytes = 0;
-        std::vector<size_t> off_pts(gn), off_rows(gn);
+        std::vector<size_t> off_pts(gn), off_rows(gn), off_exp(gn);
         for (int c = c0; c < c1; ++c) smax = std::max(smax, cats[c].stride);
         const size_t keyb = al256((size_t)smax * 4), histb = al256((size_t)256 * ((smax + 4095) / 4096 + 1) * 4);
         ws_bytes = 4 * keyb + histb;
@@ -843,6 +915,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             ws_bytes += al256((size_t)cats[c].stride * sizeof(SplitPt));
             off_rows[c - c0] = ws_bytes;
             ws_bytes += al256((size_t)3 * cats[c].stride * cats[c].in.lmax * sizeof(float));
+            off_exp[c - c0] = ws_bytes;
+            if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
         }
         CG_CUDA_TRY(ctx->split_ws.ensure(ws_bytes));
         char *ws = ctx->split_ws.as<char>();
@@ -866,8 +940,6 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             CG_CUDA_TRY(cudaGetLastError());
         }
         // ---- plan tables: catalogs, kz / jscale / nmax_l per catalog, items and reductions per level ----
-        int lmax_g = 0;
-        for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
         std::vector<char> host;  // packed plan
         auto put = [&host](const void *p, size_t b) {
             const size_t o = al256(host.size());
@@ -908,7 +980,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.stride = (int)P.stride;
             sc.lrows = P.in.lmax;
             sc.kzw = P.in.nmax;
-            sc.pad_ = 0;
+            sc.epitch = (P.in.lmax + 1) & ~1;
+            sc.rexp = ext ? reinterpret_cast<unsigned long long *>(ws + off_exp[c - c0]) : nullptr;
+            sc.eset = ext ? exp_set_words(P) : 0;
             sc.kz = nullptr;  // patched below, once the plan buffer's address is known
             sc.jscale = nullptr;
             sc.nmax_l = nullptr;
@@ -1065,7 +1139,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                             if (l >= lmax_g) continue;
                             const int ni = S.item0[l + 1] - S.item0[l];
                             if (ni == 0) continue;
-                            k_split_l<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
+                            kern<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
                             count_launch();
                         }
                         CG_CUDA_TRY(cudaGetLastError());
@@ -1096,7 +1170,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const int nr = S.red0[l + 1] - S.red0[l];
                 if (ni == 0) continue;
                 if (profile) prof_begin(ls_st);
-                k_split_l<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
+                kern<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
                 if (profile) prof_end(ls_st, S.flops[l]);
                 dim3 rg(ceil_div((int64_t)(l + 1) * S.maxn[l], 128), nr);
                 k_split_reduce<<<rg, 128, 0, ls_st>>>(partial, l + 1,
