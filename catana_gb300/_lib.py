@@ -48,6 +48,11 @@ SIGNATURES = {
     "catana_gpu_sfb_raw_batched": (ctypes.c_int, [_P, _I32, _U32, _D, _P]),
     "catana_gpu_sfb_raw_batched_dev": (ctypes.c_int, [_P, _I32, _U32, _D, _P, _P]),
     "catana_gpu_batch_waves": (ctypes.c_double, []),
+    "catana_gpu_accum_create": (ctypes.c_int, [_U16, _U16, _D, _U32, _P]),
+    "catana_gpu_accum_add_f32": (ctypes.c_int, [_P, _P, _P, _I64]),
+    "catana_gpu_accum_add": (ctypes.c_int, [_P, _P, _P, _I64]),
+    "catana_gpu_accum_finish": (ctypes.c_int, [_P, _P, _P, _P]),
+    "catana_gpu_accum_destroy": (ctypes.c_int, [_P]),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_bin_points": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
     "catana_gpu_ang2pix_ring": (ctypes.c_int, [_I64, _P, _P, _I64, _P, _P]),

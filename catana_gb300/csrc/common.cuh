@@ -78,6 +78,7 @@ struct DeviceContext {
     std::map<std::string, double> split_tuned;  // autotuned waves per catalog set
     double split_last_waves = 0.0;
     cudaStream_t capture_stream = nullptr;      // stream the split level loop is captured on
+    cudaEvent_t split_ws_event = nullptr;       // end of the last split run (orders workspace reuse across streams)
     DevBuf hp_ws;      // HEALPix workspace
     // cache keys
     int coef_lmax = -1;
@@ -120,6 +121,9 @@ catana_status_t ensure_coefs(DeviceContext *ctx, int lmax, cudaStream_t st);
 struct SplitCatInput {
     const double *pts = nullptr;  // n x 3 (r, theta, phi)
     const double *w = nullptr;    // optional weights
+    const float *pts32 = nullptr; // or: float32 records (r, theta, phi) and weights
+    const float *w32 = nullptr;
+    double max_r = -1.0, max_w = -1.0;  // >= 0: extents known to the caller (skips a read-back)
     int64_t n = 0;
     int lmax = 0, nmax = 0;
     double rmax = 1.0;

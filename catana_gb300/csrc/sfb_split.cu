@@ -566,7 +566,8 @@ __global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const
 // Point preparation, in radius-sorted order: float-float r, cos(theta), sin(theta);
 // e^{i phi} in FP32; the 64-bit phase fraction; FP32 weights.  Flags radii that are
 // negative or not finite.  Records past n (padding to whole tiles) are zeroed.
-__global__ void k_split_prep(const double *__restrict__ pts, const double *__restrict__ w,
+template <typename T>
+__global__ void k_split_prep(const T *__restrict__ pts, const T *__restrict__ w,
                              const uint32_t *__restrict__ perm, int64_t n, int64_t npad, SplitPt *out, int *err) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= npad) return;
@@ -578,7 +579,7 @@ __global__ void k_split_prep(const double *__restrict__ pts, const double *__res
         return;
     }
     const int64_t j = perm[i];
-    const double r = pts[3 * j], th = pts[3 * j + 1], ph = pts[3 * j + 2];
+    const double r = (double)pts[3 * j], th = (double)pts[3 * j + 1], ph = (double)pts[3 * j + 2];
     if (!(r >= 0.0) || !isfinite(r)) *err = CATANA_ERR_DOMAIN;
     double st, ct, sp, cp;
     sincos(th, &st, &ct);
@@ -601,24 +602,26 @@ __global__ void k_split_prep(const double *__restrict__ pts, const double *__res
 }
 
 // radius keys for the sort: 16-bit quantisation of r / max_r, and the identity payload
-__global__ void k_split_keys(const double *__restrict__ pts, int64_t n, double inv_rmax, uint32_t *keys,
+template <typename T>
+__global__ void k_split_keys(const T *__restrict__ pts, int64_t n, double inv_rmax, uint32_t *keys,
                              uint32_t *vals) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double q = pts[3 * i] * inv_rmax * 65536.0;
+    const double q = (double)pts[3 * i] * inv_rmax * 65536.0;
     keys[i] = q >= 65535.0 ? 65535u : (q > 0.0 ? (uint32_t)q : 0u);
     vals[i] = (uint32_t)i;
 }
 
 // max(r) and max(|w|) as IEEE bit patterns of non-negative doubles
-__global__ void k_split_maxes(const double *__restrict__ pts, const double *__restrict__ w, int64_t n,
+template <typename T>
+__global__ void k_split_maxes(const T *__restrict__ pts, const T *__restrict__ w, int64_t n,
                               unsigned long long *out) {
     double mr = 0.0, mw = w ? 0.0 : 1.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double r = pts[3 * i];
+        const double r = (double)pts[3 * i];
         if (r > mr) mr = r;
         if (w) {
-            const double a = fabs(w[i]);
+            const double a = fabs((double)w[i]);
             if (a > mw) mw = a;
         }
     }
@@ -830,24 +833,35 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     const int nc = (int)cats.size();
     CG_CUDA_TRY(ctx->cat_scratch.ensure((size_t)16 * nc));
     unsigned long long *mx = ctx->cat_scratch.as<unsigned long long>();
-    CG_CUDA_TRY(cudaMemsetAsync(mx, 0, (size_t)16 * nc, st));
-    for (int c = 0; c < nc; ++c) {
-        const int64_t n = cats[c].in.n;
-        k_split_maxes<<<std::min<int64_t>(4 * ctx->sm_count, ceil_div(n, 256)), 256, 0, st>>>(cats[c].in.pts,
-                                                                                             cats[c].in.w, n,
-                                                                                             mx + 2 * c);
-        count_launch();
+    // the workspace is shared by every stream that runs the split form on this device
+    if (!ctx->split_ws_event) CG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->split_ws_event, cudaEventDisableTiming));
+    else CG_CUDA_TRY(cudaStreamWaitEvent(st, ctx->split_ws_event, 0));
+    bool need = false;
+    for (auto &P : cats) need |= (P.in.max_r < 0.0 || P.in.max_w < 0.0);
+    std::vector<unsigned long long> mxh(2 * nc, 0ull);
+    if (need) {
+        CG_CUDA_TRY(cudaMemsetAsync(mx, 0, (size_t)16 * nc, st));
+        for (int c = 0; c < nc; ++c) {
+            const int64_t n = cats[c].in.n;
+            const int g = (int)std::min<int64_t>(4 * ctx->sm_count, ceil_div(n, 256));
+            if (cats[c].in.pts32)
+                k_split_maxes<float><<<g, 256, 0, st>>>(cats[c].in.pts32, cats[c].in.w32, n, mx + 2 * c);
+            else
+                k_split_maxes<double><<<g, 256, 0, st>>>(cats[c].in.pts, cats[c].in.w, n, mx + 2 * c);
+            count_launch();
+        }
+        CG_CUDA_TRY(cudaGetLastError());
+        CG_CUDA_TRY(cudaMemcpyAsync(mxh.data(), mx, (size_t)16 * nc, cudaMemcpyDeviceToHost, st));
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
     }
-    CG_CUDA_TRY(cudaGetLastError());
-    std::vector<unsigned long long> mxh(2 * nc);
-    CG_CUDA_TRY(cudaMemcpyAsync(mxh.data(), mx, (size_t)16 * nc, cudaMemcpyDeviceToHost, st));
-    CG_CUDA_TRY(cudaStreamSynchronize(st));
     int lmax_all = 0;
     double zmax = 0.0;
     for (int c = 0; c < nc; ++c) {
         CatPlan &P = cats[c];
         memcpy(&P.max_r, &mxh[2 * c], 8);
         memcpy(&P.max_w, &mxh[2 * c + 1], 8);
+        if (P.in.max_r >= 0.0) P.max_r = P.in.max_r;  // extents given by the caller
+        if (P.in.max_w >= 0.0) P.max_w = P.in.max_w;
         if (!(P.max_w > 0.0)) P.max_w = 1.0;
         const int L = P.in.lmax, M = P.in.nmax;
         P.kh.resize((size_t)L * M);
@@ -928,14 +942,22 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             CatPlan &P = cats[c];
             const int64_t n = P.in.n;
             SplitPt *spts = reinterpret_cast<SplitPt *>(ws + off_pts[c - c0]);
-            k_split_keys<<<ceil_div(n, 256), 256, 0, st>>>(P.in.pts, n, P.max_r > 0.0 ? 1.0 / P.max_r : 0.0, keys,
-                                                           perm);
+            const double inv_r = P.max_r > 0.0 ? 1.0 / P.max_r : 0.0;
+            if (P.in.pts32)
+                k_split_keys<float><<<ceil_div(n, 256), 256, 0, st>>>(P.in.pts32, n, inv_r, keys, perm);
+            else
+                k_split_keys<double><<<ceil_div(n, 256), 256, 0, st>>>(P.in.pts, n, inv_r, keys, perm);
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
             s = radix_sort_pairs(keys, perm, tk, tv, n, 16, hist, st);
             if (s != CATANA_OK) return s;
             const int64_t npad = P.ntiles * KT;
-            k_split_prep<<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts, P.in.w, perm, n, npad, spts, err_dev);
+            if (P.in.pts32)
+                k_split_prep<float><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts32, P.in.w32, perm, n, npad, spts,
+                                                                         err_dev);
+            else
+                k_split_prep<double><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts, P.in.w, perm, n, npad, spts,
+                                                                          err_dev);
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
         }
@@ -1205,9 +1227,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             s = levels(true, st);
             if (s != CATANA_OK) return s;
         }
-        // the next group reuses the workspace: finish this one first
-        if (groups.size() > 1) CG_CUDA_TRY(cudaStreamSynchronize(st));
+        // the next group reuses the workspace: stream order on `st` keeps them apart
     }
+    CG_CUDA_TRY(cudaEventRecord(ctx->split_ws_event, st));
     return CATANA_OK;
 }
 

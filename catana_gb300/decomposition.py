@@ -216,6 +216,70 @@ def sfb_decomposition_batched(point_containers, lmax, nmax, rmax, kmax=None, wei
             for i, (k, c, f) in enumerate(out)]
 
 
+class SFBAccumulator(object):
+    """Raw SFB decomposition of one catalog fed in chunks (no counterpart in the
+    reference).  ``add(points, weights=None)`` takes an (N, 3) array of (r, theta,
+    phi) -- float32 (the SphericalRecord<float> layout) or float64; pinned host
+    memory (e.g. a pinned torch tensor's numpy view) lets the copy of a chunk overlap
+    the decomposition of the previous one.  ``finish(store_flmn=False)`` returns the
+    KClkk of all points added, normalised by the total count (or weight sum).
+
+        with SFBAccumulator(512, 256, 1500.0, precision="split") as acc:
+            for chunk in chunks:
+                acc.add(chunk)
+            result = acc.finish()
+    """
+
+    def __init__(self, lmax, nmax, rmax, precision="split", interpolation="auto"):
+        self.lmax = _unsigned_short(lmax, "lmax")
+        self.nmax = _unsigned_short(nmax, "nmax")
+        self.rmax = float(rmax)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib.catana_gpu_accum_create(self.lmax, self.nmax, self.rmax, _flags(interpolation, precision),
+                                                    ctypes.byref(h)), "accum_create")
+        self._h = h
+        self._keep = []  # the last chunks stay alive until the library has copied them
+
+    def add(self, points, weights=None):
+        pts = np.asarray(points)
+        f32 = pts.dtype == np.float32
+        pts = np.ascontiguousarray(pts, dtype=np.float32 if f32 else np.float64).reshape(-1, 3)
+        w = None
+        if weights is not None:
+            w = np.ascontiguousarray(weights, dtype=pts.dtype).reshape(-1)
+            if w.shape[0] != pts.shape[0]:
+                raise ValueError("weights must have one entry per point")
+        fn = _lib.lib.catana_gpu_accum_add_f32 if f32 else _lib.lib.catana_gpu_accum_add
+        _lib.check(fn(self._h, _lib.ptr(pts), _lib.ptr(w), pts.shape[0]), "accum_add")
+        self._keep = (self._keep + [(pts, w)])[-2:]
+
+    def finish(self, store_flmn=False):
+        k = np.zeros((self.lmax, self.nmax))
+        c = np.zeros((self.lmax, self.nmax))
+        f = np.zeros(int(_lib.lib.catana_gpu_flmn_size(self.lmax, self.nmax)), dtype=np.complex128) \
+            if store_flmn else None
+        _lib.check(_lib.lib.catana_gpu_accum_finish(self._h, _lib.ptr(k), _lib.ptr(c), _lib.ptr(f)), "accum_finish")
+        self._keep = []
+        return KClkk(k, c, unpack_flmn(f, self.lmax, self.nmax) if store_flmn else [])
+
+    def close(self):
+        if self._h is not None:
+            _lib.lib.catana_gpu_accum_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def compute_kln(lmax, nmax, rmax):
     """k_ln = z_{l,n} / rmax (return_types.cpp:10-20), as a (lmax, nmax) array."""
     lmax = _unsigned_short(lmax, "lmax")

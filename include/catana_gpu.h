@@ -161,6 +161,33 @@ catana_status_t catana_gpu_sfb_raw_batched_dev(const catana_catalog_t *cats, int
 /* Waves per SM the last split-form run used (the autotuned value when it tuned). */
 double catana_gpu_batch_waves(void);
 
+/* ---- chunked accumulation of one large catalog (no counterpart in the reference) --
+ * For catalogs streamed from disk or host memory in chunks (the reference's
+ * FilterStream buffers the whole catalog before decomposing it,
+ * FilterStream.cpp:100-124).  create() computes k_ln and zeroes the f sum on the
+ * device; each add() copies one chunk from host memory (pinned memory makes the copy
+ * asynchronous: the copy of chunk k+1 overlaps the decomposition of chunk k) and
+ * decomposes it on the accumulator's own streams; finish() normalises with the total
+ * point count (or weight sum), forms C_ln and writes k_ln, c_ln and optionally f_lmn
+ * (host, layouts as catana_gpu_sfb_raw).  Flags: CATANA_FORM_* (and CATANA_JL_EXACT
+ * for the plain form; JL_AUTO takes the table form, the reference's rule for any
+ * catalog of more than 1000 points).  A host chunk may be reused once the second
+ * add() after it, or finish(), has returned (pageable memory: at once).  Chunks must
+ * all carry weights or none.  finish() ends the accumulation.  An accumulator is
+ * used from one thread at a time. */
+typedef struct catana_gpu_accum *catana_gpu_accum_t;
+catana_status_t catana_gpu_accum_create(uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags,
+                                        catana_gpu_accum_t *out);
+/* chunk of n float32 (r, theta, phi) records (the SphericalRecord<float> layout that
+ * RawBinarySource reads, record_types.hpp:82-160) and optional float32 weights */
+catana_status_t catana_gpu_accum_add_f32(catana_gpu_accum_t acc, const float *points, const float *weights,
+                                         int64_t n);
+/* chunk of n float64 (r, theta, phi) records and optional weights */
+catana_status_t catana_gpu_accum_add(catana_gpu_accum_t acc, const double *points, const double *weights,
+                                     int64_t n);
+catana_status_t catana_gpu_accum_finish(catana_gpu_accum_t acc, double *k_ln, double *c_ln, double *f_lmn);
+catana_status_t catana_gpu_accum_destroy(catana_gpu_accum_t acc);
+
 /* HEALPix (pixelized) SFB decomposition.  The catalog is given binned: pixel p
  * (RING scheme) holds the radii r_sorted[pix_offsets[p] .. pix_offsets[p+1]), in
  * the order the points were added.  npix = 12 nside^2; pix_offsets has npix+1
