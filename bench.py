@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--plain-sample", type=int, default=20_000, help="points for the FP64 plain GPU comparison")
     p.add_argument("--side", type=int, default=1, help="also time the FP64 (100k, 32, 32) and HEALPix cases")
     p.add_argument("--no-extras", action="store_true", help="skip e2e/cpu/plain/accuracy legs")
+    p.add_argument("--stream-chunks", type=int, default=2,
+                   help="8M-point chunks of the streamed lmax 512 / nmax 256 survey leg (0 skips it)")
     return p.parse_args()
 
 
@@ -330,6 +332,83 @@ def batched_workload(torch, _lib, catana, sp, ncat=64, seed=4, kmax=0.2, nmax=12
     return res
 
 
+def survey_chunk(rng, n, rmax=1500.0, a=300.0):
+    """n float32 (r, theta, phi) records: radial pdf ~ r^2 exp(-(r/a)^2) truncated at
+    rmax (r = a/sqrt(2) chi_3), |theta - pi/2| < 20 deg masked out, phi uniform."""
+    out = np.empty((n, 3), dtype=np.float32)
+    got = 0
+    smin = np.sin(np.deg2rad(20.0))
+    while got < n:
+        k = n - got
+        r = a / np.sqrt(2.0) * np.sqrt((rng.standard_normal((k, 3)) ** 2).sum(1))
+        r = r[r < rmax]
+        m = r.shape[0]
+        ct = rng.uniform(smin, 1.0, m) * np.where(rng.random(m) < 0.5, -1.0, 1.0)
+        out[got:got + m, 0] = r
+        out[got:got + m, 1] = np.arccos(ct)
+        out[got:got + m, 2] = rng.uniform(0.0, 2.0 * np.pi, m)
+        got += m
+    return out
+
+
+def streamed_workload(torch, _lib, catana, chunks=2, chunk=8_000_000, L=512, M=256, seed=4):
+    """Large masked survey through the chunked accumulator: float32 (r, theta, phi)
+    records in pinned host memory, 8M-point chunks, lmax 512, nmax 256, split form
+    (the full survey has 100M points = 13 such chunks; the rate per point is the same
+    for every chunk, so a bounded number of chunks is timed).  The timed region is
+    create + every add (host-to-device copy overlapped with the previous chunk's
+    decomposition) + finish (normalisation, C_ln, copies back)."""
+    rng = np.random.default_rng(seed)
+    host = []
+    for _ in range(chunks):
+        t = torch.empty((chunk, 3), dtype=torch.float32, pin_memory=True)
+        t.numpy()[:] = survey_chunk(rng, chunk)
+        host.append(t)
+    warm = survey_chunk(rng, 50000)
+    with catana.SFBAccumulator(L, M, 1500.0, precision="split") as acc:  # builds the j_l tables once
+        acc.add(warm)
+        acc.finish()
+    torch.cuda.synchronize()
+    _lib.lib.catana_gpu_profile_enable(1)
+    t0 = time.perf_counter()
+    with catana.SFBAccumulator(L, M, 1500.0, precision="split") as acc:
+        for t in host:
+            acc.add(t.numpy())
+        res = acc.finish()
+    dt = time.perf_counter() - t0
+    _lib.lib.catana_gpu_profile_enable(0)
+    kms, kn, kfl = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_double()
+    _lib.check(_lib.lib.catana_gpu_profile_report(ctypes.byref(kms), ctypes.byref(kn), ctypes.byref(kfl)))
+    pm = float(chunks * chunk) * modes(L, M)
+    out = {"value": pm / dt, "unit": UNIT, "seconds": dt, "points": chunks * chunk, "chunk": chunk, "lmax": L,
+           "nmax": M, "input": "float32 (r, theta, phi), pinned host memory",
+           "contraction_kernel_s": kms.value / 1e3, "contraction_tflops_algorithmic": kfl.value / (kms.value / 1e3) / 1e12,
+           "c_ln_finite": bool(np.isfinite(res.c_ln).all())}
+    # FP64 plain form on a 20k-point subsample (interpolated j_l, the reference's rule)
+    sub = host[0].numpy()[:20000].astype(np.float64)
+    pc = catana.PointContainer(sub)
+    catana.sfb_decomposition(pc, L, M, 1500.0, False, False)
+    t0 = time.perf_counter()
+    catana.sfb_decomposition(pc, L, M, 1500.0, False, False)
+    tp = time.perf_counter() - t0
+    out["plain_fp64_20k_value"] = 20000 * modes(L, M) / tp
+    out["split_over_plain"] = out["value"] / out["plain_fp64_20k_value"]
+    # C_l error of the split form against FP64 with exact j_l on 1500 points
+    e = host[0].numpy()[:1500].astype(np.float64)
+    pe = catana.PointContainer(e)
+    rs = catana.sfb_decomposition(pe, L, M, 1500.0, False, False, precision="split")
+    rp = catana.sfb_decomposition(pe, L, M, 1500.0, False, False, interpolation="off")
+    rel = np.abs(rs.c_ln - rp.c_ln) / np.abs(rp.c_ln)
+    keep = rp.c_ln >= 1e-40 * rp.c_ln.max()  # below: j_l(k r) < ~1e-20 of its envelope at every point
+    out["accuracy_1500pts"] = {"c_ln_rel_err_median": float(np.median(rel)),
+                               "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
+                               "c_ln_rel_err_p99_modes_above_1e-40_cmax": float(np.percentile(rel[keep], 99)),
+                               "modes_below_1e-40_cmax": float(1.0 - keep.mean()),
+                               "reference": "FP64 plain path, exact j_l"}
+    del host
+    return out
+
+
 def workload_config(a):
     return {"workload": "raw SFB %s form: %d points uniform in a ball rmax=%g, weights U[0.5,1.5], lmax=%d, "
                         "nmax=%d, seed %d" % (a.form, a.points, a.rmax, a.lmax, a.nmax, a.seed),
@@ -527,6 +606,9 @@ def main():
         if a.side:
             out["side"] = side_workloads(torch, _lib, catana, sp)
             out["side"]["batched_64_catalogs_kmax0.2_split"] = batched_workload(torch, _lib, catana, sp)
+            if a.stream_chunks > 0:
+                out["side"]["streamed_survey_l512_n256_split"] = streamed_workload(torch, _lib, catana,
+                                                                                  chunks=a.stream_chunks)
         # ---- CPU baseline: the oracle's OpenMP restatement on a bounded sample ----
         cs = min(a.cpu_sample, a.points)
         v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)

@@ -50,7 +50,8 @@ struct DevBuf {
 // coefficients and the largest |j_l| per l.
 struct SplitCache {
     int lmax = -1, nmax = -1, nint = -1;
-    std::vector<double> maxj;
+    std::vector<double> maxj;   // 1.05 max |j_l| (first maximum)
+    std::vector<double> zpeak;  // where that maximum sits (j_l rises monotonically below)
 };
 
 // Per-device state: workspace and cached tables.  Guarded by `mu`.

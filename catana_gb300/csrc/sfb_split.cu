@@ -80,7 +80,7 @@ constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS + SM_STEXP;  // P_{l-1}, P
 constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
 constexpr uint32_t SM_TAB = NINT_MAX * 32;
 constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;
-constexpr uint32_t OFF_COEF = OFF_KZ + NHALF * 8;
+constexpr uint32_t OFF_COEF = OFF_KZ + NHALF * 16;
 constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
@@ -110,8 +110,7 @@ struct SplitCat {
     int epitch;             // exponent words per tile (lrows rounded up to even)
     unsigned long long *rexp;  // extended range: three exponent sets [tile][lrows], set k at rexp + k * eset
     int64_t eset;           // words per exponent set
-    const float2 *kz;       // [l][kzw]: k_ln / H as float-float
-    const float *jscale;    // [l]: 2^sJ
+    const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
 };
 
@@ -175,8 +174,6 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const int nh0 = item.n0;
     const int nmax = min(NHALF, cat.nmax_l[l] - nh0);  // radial orders of this half
     const bool wrows = (nh0 == 0);                      // the first half writes the Legendre rows
-    const float jscale = cat.jscale[l];
-    const float inv_scale = 1.0f / (jscale * Y_SCALE);
     const int ncols = 2 * mcount;
     const int ncols_pad = (ncols + 15) & ~15;
     uint32_t half_cols = 32;
@@ -184,9 +181,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const uint32_t tcols = 2 * half_cols;  // D_tile at column 0, D_acc at column half_cols
 
     float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
-    float2 *s_kz = reinterpret_cast<float2 *>(sm + OFF_KZ);
+    float4 *s_kz = reinterpret_cast<float4 *>(sm + OFF_KZ);
     float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);
-    const float2 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
+    const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
     for (int t = tid; t < nmax; t += NTHR) s_kz[t] = kz_row[t];
     for (int t = tid; t < mcount; t += NTHR) s_coef[t] = a.coef[mb0 + t];
@@ -289,7 +286,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         ++folds;
     };
 
-    // partial[cta] (+)= D_acc * inv_scale, then the next fold restarts D_acc
+    // partial[cta] (+)= D_acc / (2^s_ln 2^12) (lane n), then the next fold restarts D_acc
     auto flush = [&]() {
         tc05::fence_after();
         const int qd = warp & 3, cq = warp >> 2;
@@ -299,6 +296,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             tc05::tmem_ld16(d_acc + ((uint32_t)(qd * 32) << 16) + gi * 16, v);
             tc05::tmem_wait_ld();
             if (lane_n < nmax) {
+                const float inv_scale = s_kz[lane_n].w;
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int col = gi * 16 + j;
@@ -345,7 +343,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             if (valid) {
                 rh = pt.r_hi;
                 rl = pt.r_lo;
-                wj = pt.w * jscale;
+                wj = pt.w;
             }
             const int n0 = 8 * g;
             float v[8];
@@ -354,7 +352,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                 const int n = n0 + k;
                 float val = 0.f;
                 if (valid && n < nmax) {
-                    const float2 kk = s_kz[n];
+                    const float4 kk = s_kz[n];
                     const float p = rh * kk.x;
                     float e = fmaf(rh, kk.x, -p);
                     e = fmaf(rh, kk.y, e);
@@ -373,7 +371,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                     jv = fmaf(jv, uu, c0.z);
                     jv = fmaf(jv, uu, c0.y);
                     jv = fmaf(jv, uu, c0.x);
-                    val = jv * wj;
+                    val = jv * (wj * kk.z);
                 }
                 v[k] = val;
             }
@@ -771,14 +769,21 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
     CG_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(tab) + tab_bytes, co.data(), coef_bytes,
                                 cudaMemcpyHostToDevice, st));
     C.maxj.assign(lmax, 1.0);
-    for (int l = 1; l < lmax; ++l) {  // largest |j_l|: around the first maximum, z ~ l + 0.8 l^(1/3)
-        double mj = 0.0;
+    C.zpeak.assign(lmax, 0.0);
+    for (int l = 1; l < lmax; ++l) {  // largest |j_l|: its first maximum, z ~ l + 0.8 l^(1/3)
+        double mj = 0.0, zp = 0.0;
         const double zc = l + 0.8 * std::cbrt((double)l);
         for (int q = -200; q <= 400; ++q) {
             const double z = zc + 0.02 * q;
-            if (z > 0) mj = std::max(mj, std::fabs(sbessel_jl(l, z)));
+            if (z <= 0) continue;
+            const double v = std::fabs(sbessel_jl(l, z));
+            if (v > mj) {
+                mj = v;
+                zp = z;
+            }
         }
         C.maxj[l] = 1.05 * mj;
+        C.zpeak[l] = zp - 0.05;  // j_l increases monotonically below this
     }
     CG_CUDA_TRY(cudaStreamSynchronize(st));
     tmp.release();
@@ -969,24 +974,30 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             memcpy(host.data() + o, p, b);
             return o;
         };
-        std::vector<size_t> o_kz(gn), o_js(gn), o_nl(gn);
+        std::vector<size_t> o_kz(gn), o_nl(gn);
         for (int c = c0; c < c1; ++c) {
             CatPlan &P = cats[c];
             const int L = P.in.lmax, M = P.in.nmax;
-            std::vector<float2> kz((size_t)L * M);
-            for (size_t t = 0; t < kz.size(); ++t) {
-                float hi, lo;
-                split_ff(P.kh[t] / H, hi, lo);
-                kz[t] = make_float2(hi, lo);
-            }
-            std::vector<float> js(L);
-            for (int l = 0; l < L; ++l) {
-                const double mj = l < (int)ctx->split_cache.maxj.size() ? ctx->split_cache.maxj[l] : 1.0;
-                const int e = (int)std::floor(std::log2(32768.0 / (mj * P.max_w)));
-                js[l] = (float)std::ldexp(1.0, std::max(-60, std::min(100, e)));
-            }
-            o_kz[c - c0] = put(kz.data(), kz.size() * sizeof(float2));
-            o_js[c - c0] = put(js.data(), js.size() * sizeof(float));
+            // J scale per (l, n): a power of two bringing max |w j_l(k_ln r)| over the
+            // catalog's radii into [2^14, 2^15) -- j_l rises monotonically up to its
+            // first maximum, so below it the largest radius sets the bound.  Modes whose
+            // arguments stay deep below l keep their J values normal in FP16.
+            std::vector<float4> kz((size_t)L * M);
+            const SplitCache &C = ctx->split_cache;
+            for (int l = 0; l < L; ++l)
+                for (int n = 0; n < M; ++n) {
+                    const size_t t = (size_t)l * M + n;
+                    float hi, lo;
+                    split_ff(P.kh[t] / H, hi, lo);
+                    const double zl = P.kh[t] * P.max_r;
+                    double mj = C.maxj[l];
+                    if (l > 0 && zl < C.zpeak[l]) mj = std::min(mj, std::fabs(sbessel_jl(l, zl)));
+                    mj = std::max(mj, 1e-300);
+                    const int e = std::max(-60, std::min(110, (int)std::floor(std::log2(32768.0 / (mj * P.max_w)))));
+                    const double js = std::ldexp(1.0, e);
+                    kz[t] = make_float4(hi, lo, (float)js, (float)(1.0 / (js * Y_SCALE)));
+                }
+            o_kz[c - c0] = put(kz.data(), kz.size() * sizeof(float4));
             o_nl[c - c0] = put(P.nmax_l.data(), P.nmax_l.size() * sizeof(int));
         }
         // catalog descriptors (fixed for the group)
@@ -1006,7 +1017,6 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.rexp = ext ? reinterpret_cast<unsigned long long *>(ws + off_exp[c - c0]) : nullptr;
             sc.eset = ext ? exp_set_words(P) : 0;
             sc.kz = nullptr;  // patched below, once the plan buffer's address is known
-            sc.jscale = nullptr;
             sc.nmax_l = nullptr;
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
@@ -1109,8 +1119,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             host.resize(std::max(host.size(), total));
             for (int c = c0; c < c1; ++c) {
                 SplitCat *sc = reinterpret_cast<SplitCat *>(host.data() + o_cats) + (c - c0);
-                sc->kz = reinterpret_cast<const float2 *>(pd + o_kz[c - c0]);
-                sc->jscale = reinterpret_cast<const float *>(pd + o_js[c - c0]);
+                sc->kz = reinterpret_cast<const float4 *>(pd + o_kz[c - c0]);
                 sc->nmax_l = reinterpret_cast<const int *>(pd + o_nl[c - c0]);
             }
             if (ib) memcpy(host.data() + o_items, S.items.data(), ib);
