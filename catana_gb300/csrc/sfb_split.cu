@@ -79,8 +79,10 @@ constexpr uint32_t SM_STEXP = 2 * MBLK * 8;            // row exponent words of 
 constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS + SM_STEXP;  // P_{l-1}, P_{l-2}, the points, exponents
 constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
 constexpr uint32_t SM_TAB = NINT_MAX * 32;
-constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;
-constexpr uint32_t OFF_COEF = OFF_KZ + NHALF * 16;
+constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;          // per n pair: (kz_hi, kz_lo) x 2, then J scales
+constexpr uint32_t OFF_JS = OFF_KZ + NHALF * 8;         // J scale 2^s_ln per n
+constexpr uint32_t OFF_INV = OFF_JS + NHALF * 4;        // readout 2^-s_ln 2^-12 per n
+constexpr uint32_t OFF_COEF = OFF_INV + NHALF * 4;      // recurrence coefficients, m pairs
 constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
@@ -144,6 +146,30 @@ __device__ __forceinline__ void store_split8(uint8_t *hi_base, uint8_t *lo_base,
     *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
+// Same for four value pairs (columns 2k, 2k+1 from v[k]) with packed FP32 arithmetic.
+__device__ __forceinline__ void store_split8p(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, float2 v0, float2 v1,
+                                              float2 v2, float2 v3) {
+    const float2 v[4] = {v0, v1, v2, v3};
+    uint32_t h[4], o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __half2 hh = __float22half2_rn(v[k]);
+        const float2 hf = __half22float2(hh);
+        const float2 lo = __fadd2_rn(v[k], make_float2(-hf.x, -hf.y));
+        __half2 ll = __float22half2_rn(lo);
+        h[k] = *reinterpret_cast<uint32_t *>(&hh);
+        o[k] = *reinterpret_cast<uint32_t *>(&ll);
+    }
+    *reinterpret_cast<uint4 *>(hi_base + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// Y column order inside each 8-column group of complex m0..m0+3:
+//   Re m0, Re m0+1, Im m0, Im m0+1, Re m0+2, Re m0+3, Im m0+2, Im m0+3
+// (value pairs of consecutive m stay adjacent for the packed arithmetic).
+__host__ __device__ __forceinline__ int col_m(int col) { return 4 * (col >> 3) + (col & 1) + 2 * ((col >> 2) & 1); }
+__host__ __device__ __forceinline__ int col_ri(int col) { return (col >> 1) & 1; }
+
 // e^{i m phi} from the 64-bit phase fraction u = phi / 2pi:  (cos, sin)(2 pi frac(m u))
 __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c, float &s) {
     const unsigned long long t = (unsigned long long)m * u;  // mod 2^64: frac(m u) exactly
@@ -181,12 +207,28 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     const uint32_t tcols = 2 * half_cols;  // D_tile at column 0, D_acc at column half_cols
 
     float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
-    float4 *s_kz = reinterpret_cast<float4 *>(sm + OFF_KZ);
-    float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);
+    float4 *s_kzp = reinterpret_cast<float4 *>(sm + OFF_KZ);  // n pair j: (hi n, hi n+1, lo n, lo n+1)
+    float *s_js = reinterpret_cast<float *>(sm + OFF_JS);
+    float *s_inv = reinterpret_cast<float *>(sm + OFF_INV);
+    float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
-    for (int t = tid; t < nmax; t += NTHR) s_kz[t] = kz_row[t];
-    for (int t = tid; t < mcount; t += NTHR) s_coef[t] = a.coef[mb0 + t];
+    // radial orders past this half's count get k = 0 and J scale 0: their J rows are zero
+    for (int t = tid; t < NHALF / 2; t += NTHR) {
+        const float4 ka = 2 * t < nmax ? kz_row[2 * t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 kb = 2 * t + 1 < nmax ? kz_row[2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_kzp[t] = make_float4(ka.x, kb.x, ka.y, kb.y);
+        s_js[2 * t] = ka.z;
+        s_js[2 * t + 1] = kb.z;
+        s_inv[2 * t] = ka.w;
+        s_inv[2 * t + 1] = kb.w;
+    }
+    for (int t = tid; t < (mcount + 1) / 2; t += NTHR) {
+        const float4 ca = a.coef[mb0 + 2 * t];
+        const float4 cb = 2 * t + 1 < mcount ? a.coef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_coef[2 * t] = make_float4(ca.x, cb.x, ca.y, cb.y);
+        s_coef[2 * t + 1] = make_float4(ca.z, cb.z, ca.w, cb.w);
+    }
     if (tid == 0) {
         tc05::mbar_init(&mbar[0], 1);
         tc05::mbar_init(&mbar[1], 1);
@@ -277,7 +319,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             tc05::tmem_wait_ld();
             if (!acc_fresh) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) vt[j] = __float_as_uint(__uint_as_float(vt[j]) + __uint_as_float(va[j]));
+                for (int j = 0; j < 16; j += 2) {
+                    const float2 sm2 = __fadd2_rn(make_float2(__uint_as_float(vt[j]), __uint_as_float(vt[j + 1])),
+                                                  make_float2(__uint_as_float(va[j]), __uint_as_float(va[j + 1])));
+                    vt[j] = __float_as_uint(sm2.x);
+                    vt[j + 1] = __float_as_uint(sm2.y);
+                }
             }
             tc05::tmem_st16(d_acc + lane_off + gi * 16, vt);
         }
@@ -296,13 +343,14 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             tc05::tmem_ld16(d_acc + ((uint32_t)(qd * 32) << 16) + gi * 16, v);
             tc05::tmem_wait_ld();
             if (lane_n < nmax) {
-                const float inv_scale = s_kz[lane_n].w;
+                const float inv_scale = s_inv[lane_n];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int col = gi * 16 + j;
-                    if (col < ncols) {
+                    const int ml = col_m(col);
+                    if (ml < mcount) {
                         const float d = __uint_as_float(v[j]) * inv_scale;
-                        float *p = partial_cta + (size_t)col * 128 + lane_n;
+                        float *p = partial_cta + (size_t)(2 * ml + col_ri(col)) * 128 + lane_n;
                         *p = first_flush ? d : (*p + d);
                     }
                 }
@@ -335,137 +383,155 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         const unsigned long long *stge2 = stge1 + MBLK;
         const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
                                                                 2 * SM_STROW + q * 48);
-        const int64_t i = t * KT + q;
-        const bool valid = i < cat.n;
-        // ---- J tile: n = 8 g .. 8 g + 7 ----
+        const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
+        // ---- J tile: n = 8 g .. 8 g + 7 (zero past this half's count) ----
         {
-            float rh = 0.f, rl = 0.f, wj = 0.f;
-            if (valid) {
-                rh = pt.r_hi;
-                rl = pt.r_lo;
-                wj = pt.w;
-            }
+            const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
+            const float2 w2 = make_float2(pt.w, pt.w);
             const int n0 = 8 * g;
-            float v[8];
+            float2 v[4];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const int n = n0 + k;
-                float val = 0.f;
-                if (valid && n < nmax) {
-                    const float4 kk = s_kz[n];
-                    const float p = rh * kk.x;
-                    float e = fmaf(rh, kk.x, -p);
-                    e = fmaf(rh, kk.y, e);
-                    e = fmaf(rl, kk.x, e);
-                    const float fl = rintf(p);
-                    int idx = (int)fl;
-                    const float uu = (p - fl) + e;  // in [-1/2, 1/2]
-                    if ((unsigned)idx >= (unsigned)a.nint) {
-                        *a.err = CATANA_ERR_DOMAIN;
-                        idx = idx < 0 ? 0 : a.nint - 1;
-                    }
-                    const float4 c0 = s_tab[2 * idx], c1 = s_tab[2 * idx + 1];
-                    float jv = fmaf(c1.z, uu, c1.y);
-                    jv = fmaf(jv, uu, c1.x);
-                    jv = fmaf(jv, uu, c0.w);
-                    jv = fmaf(jv, uu, c0.z);
-                    jv = fmaf(jv, uu, c0.y);
-                    jv = fmaf(jv, uu, c0.x);
-                    val = jv * (wj * kk.z);
-                }
-                v[k] = val;
+            for (int k = 0; k < 4; ++k) {
+                const int n = n0 + 2 * k;
+                const float4 kk = s_kzp[n >> 1];
+                const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
+                // z = r k as float-float: p + e
+                const float2 p = __fmul2_rn(rh2, kx);
+                float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
+                e = __ffma2_rn(rh2, ky, e);
+                e = __ffma2_rn(rl2, kx, e);
+                const float2 fl = make_float2(rintf(p.x), rintf(p.y));
+                const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);  // in [-1/2, 1/2]
+                // radii are checked on the host against the table's extent; clamp regardless
+                const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
+                const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
+                const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
+                float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
+                ja = fmaf(ja, uu.x, a1.x);
+                jb = fmaf(jb, uu.y, b1.x);
+                ja = fmaf(ja, uu.x, a0.w);
+                jb = fmaf(jb, uu.y, b0.w);
+                ja = fmaf(ja, uu.x, a0.z);
+                jb = fmaf(jb, uu.y, b0.z);
+                ja = fmaf(ja, uu.x, a0.y);
+                jb = fmaf(jb, uu.y, b0.y);
+                ja = fmaf(ja, uu.x, a0.x);
+                jb = fmaf(jb, uu.y, b0.x);
+                const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
+                v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
             }
-            store_split8(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v);
+            store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
         }
-        // ---- Y tile: local m = mlo .. mhi-1 of this block (groups of 4 complex = 8 columns) ----
+        // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
         if (mlo < mhi) {
-            float xh = 0.f, xl = 0.f, sh = 0.f, sl = 0.f, c1 = 1.f, s1 = 0.f;
-            unsigned long long uph = 0ull;
-            if (valid) {
-                xh = pt.x_hi;
-                xl = pt.x_lo;
-                sh = pt.s_hi;
-                sl = pt.s_lo;
-                c1 = pt.cphi;
-                s1 = pt.sphi;
-                uph = pt.u;
-            }
-            float cm, smv;
-            phase_seed(uph, mb0 + mlo, cm, smv);
+            const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
+            // e^{i m phi} for the pair (m, m+1): seed m, one rotation by e^{i phi}; pairs then
+            // advance by e^{2 i phi}.  nsm holds -sin.
+            float cma, sma;
+            phase_seed(pt.u, mb0 + mlo, cma, sma);
+            float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
+            float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
+            const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
+            const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
+            const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
+            const float2 yu2 = make_float2(Y_UNSCALE, Y_UNSCALE);
 #pragma unroll
             for (int gq = 0; gq < 2; ++gq) {
                 const int ml0 = mlo + 4 * gq;
                 if (ml0 < mhi) {
-                    float v[8];
+                    float2 yr[2], yi[2];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int ml = ml0 + k;
+                    for (int hp = 0; hp < 2; ++hp) {
+                        const int ml = ml0 + 2 * hp;  // even local m
                         const int m = mb0 + ml;
-                        float yr = 0.f, yi = 0.f;
-                        if (ml < mhi) {  // warp-uniform
-                            float P = 0.f;
-                            unsigned e = 0;
-                            if (valid) {
-                                if (l == 0) {
-                                    P = P00_SCALED;
-                                } else {
-                                    const float4 c = s_coef[ml];
-                                    float p1 = stg1[ml * KT + q];
-                                    const bool sect = (m == l);
-                                    const float xa = sect ? sh : xh, xb = sect ? sl : xl;
-                                    float p2 = (m <= l - 2) ? stg2[ml * KT + q] : 0.f;
-                                    if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
-                                        const unsigned long long w1 = stge1[sect ? ml - 1 : ml];
-                                        e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
-                                        if (m <= l - 2) {
-                                            const unsigned long long w2 = stge2[ml];
-                                            const unsigned e2 =
-                                                (unsigned)((w2 >> q) & 1ull) | ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
-                                            // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                            if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
-                                        }
-                                    }
-                                    const float tt = fmaf(xa, p1, xb * p1);
-                                    const float bb = fmaf(c.w, p2, c.z * p2);
-                                    const float vv = fmaf(c.y, tt, -bb);
-                                    P = fmaf(c.x, tt, vv);
-                                    if (EXT) {
-                                        const float ap = fabsf(P);
-                                        if (sect) {
-                                            if (ap < 0x1p-40f) {
-                                                if (e < 3) {
-                                                    P = P * 0x1p64f * 0x1p64f;
-                                                    ++e;
-                                                } else {
-                                                    P = 0.f;  // below 2^-520: no contribution within lmax
-                                                }
+                        float2 P;
+                        if (!EXT && m + 1 <= l - 2 && ml + 1 < mcount) {
+                            // both m take the plain three-term step: packed arithmetic
+                            const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
+                            const float2 p1 = make_float2(stg1[ml * KT + q], stg1[(ml + 1) * KT + q]);
+                            const float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
+                            const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
+                            const float2 bb =
+                                __ffma2_rn(make_float2(cb.z, cb.w), p2, __fmul2_rn(make_float2(cb.x, cb.y), p2));
+                            const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
+                            P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                            if (wrows) {
+                                st0[(int64_t)m * stride + i] = P.x;
+                                st0[(int64_t)(m + 1) * stride + i] = P.y;
+                            }
+                        } else {
+                            // sectoral (m = l), m = l - 1, the block's last odd m, or extended range
+                            const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
+                            float pv[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const int mlh = ml + h, mh = m + h;
+                                float Pq = 0.f;
+                                unsigned e = 0;
+                                if (mlh < mhi) {  // warp-uniform
+                                    if (l == 0) {
+                                        Pq = P00_SCALED;
+                                    } else {
+                                        const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
+                                        const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
+                                        const float p1 = stg1[mlh * KT + q];
+                                        const bool sect = (mh == l);
+                                        const float xa = sect ? sh : xh, xb = sect ? sl : xl;
+                                        float p2 = (mh <= l - 2) ? stg2[mlh * KT + q] : 0.f;
+                                        if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
+                                            const unsigned long long w1 = stge1[sect ? mlh - 1 : mlh];
+                                            e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
+                                            if (mh <= l - 2) {
+                                                const unsigned long long w2 = stge2[mlh];
+                                                const unsigned e2 = (unsigned)((w2 >> q) & 1ull) |
+                                                                    ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
+                                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                                if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
                                             }
-                                        } else if (e > 0 && ap > 0x1p40f) {
-                                            P = P * 0x1p-64f * 0x1p-64f;
-                                            --e;
+                                        }
+                                        const float tt = fmaf(xa, p1, xb * p1);
+                                        const float bb = fmaf(B_lo, p2, B_hi * p2);
+                                        const float vv = fmaf(A_lo, tt, -bb);
+                                        Pq = fmaf(A_hi, tt, vv);
+                                        if (EXT) {
+                                            const float ap = fabsf(Pq);
+                                            if (sect) {
+                                                if (ap < 0x1p-40f) {
+                                                    if (e < 3) {
+                                                        Pq = Pq * 0x1p64f * 0x1p64f;
+                                                        ++e;
+                                                    } else {
+                                                        Pq = 0.f;  // below 2^-520: no contribution within lmax
+                                                    }
+                                                }
+                                            } else if (e > 0 && ap > 0x1p40f) {
+                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                --e;
+                                            }
                                         }
                                     }
+                                    if (wrows) st0[(int64_t)mh * stride + i] = Pq;
+                                    if (EXT && wrows) {
+                                        const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
+                                        const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
+                                        if (lane == 0) ex0[t * cat.epitch + mh] = ((unsigned long long)b1w << 32) | b0w;
+                                    }
+                                    if (EXT && e != 0) Pq = 0.f;  // below 2^-188: no contribution
                                 }
-                                if (wrows) st0[(int64_t)m * stride + i] = P;
+                                pv[h] = Pq;
                             }
-                            if (EXT && wrows) {
-                                const unsigned b0 = __ballot_sync(0xffffffffu, e & 1u);
-                                const unsigned b1 = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
-                                if (lane == 0) ex0[t * cat.epitch + m] = ((unsigned long long)b1 << 32) | b0;
-                            }
-                            const float Pu = (EXT && e != 0) ? 0.f : P * Y_UNSCALE;
-                            yr = Pu * cm;
-                            yi = -Pu * smv;
+                            P = make_float2(pv[0], pv[1]);
                         }
-                        v[2 * k] = yr;
-                        v[2 * k + 1] = yi;
-                        // rotate e^{i m phi} -> e^{i (m+1) phi}
-                        const float nc = fmaf(cm, c1, -smv * s1);
-                        const float ns = fmaf(smv, c1, cm * s1);
-                        cm = nc;
-                        smv = ns;
+                        const float2 Pu = __fmul2_rn(P, yu2);
+                        yr[hp] = __fmul2_rn(Pu, cm);
+                        yi[hp] = __fmul2_rn(Pu, nsm);
+                        // e^{i (m+2) phi} = e^{i m phi} e^{2 i phi}
+                        const float2 cmn = __ffma2_rn(cm, c22, __fmul2_rn(nsm, s22));
+                        nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
+                        cm = cmn;
                     }
-                    store_split8(yhi, ylo, tc05::mn_sw128_off(2 * ml0, q, 4), v);
+                    store_split8p(yhi, ylo, tc05::mn_sw128_off(2 * ml0, q, 4), yr[0], yi[0], yr[1], yi[1]);
                 }
             }
         }
