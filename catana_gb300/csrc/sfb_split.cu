@@ -164,6 +164,23 @@ __device__ __forceinline__ void store_split8p(uint8_t *hi_base, uint8_t *lo_base
     *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
+// Columns 4j .. 4j+3 from two value pairs (8 bytes of each half).
+__device__ __forceinline__ void store_split4p(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, float2 v0, float2 v1) {
+    const float2 v[2] = {v0, v1};
+    uint32_t h[2], o[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        __half2 hh = __float22half2_rn(v[k]);
+        const float2 hf = __half22float2(hh);
+        const float2 lo = __fadd2_rn(v[k], make_float2(-hf.x, -hf.y));
+        __half2 ll = __float22half2_rn(lo);
+        h[k] = *reinterpret_cast<uint32_t *>(&hh);
+        o[k] = *reinterpret_cast<uint32_t *>(&ll);
+    }
+    *reinterpret_cast<uint2 *>(hi_base + off) = make_uint2(h[0], h[1]);
+    *reinterpret_cast<uint2 *>(lo_base + off) = make_uint2(o[0], o[1]);
+}
+
 // Y column order inside each 8-column group of complex m0..m0+3:
 //   Re m0, Re m0+1, Im m0, Im m0+1, Re m0+2, Re m0+3, Im m0+2, Im m0+3
 // (value pairs of consecutive m stay adjacent for the packed arithmetic).
@@ -242,8 +259,10 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
 
     const int64_t t0 = item.t0, t1 = item.t1;
     const int q = lane, g = warp;
-    const int MRW = (((mcount + 15) / 16) + 3) & ~3;  // m per warp, multiple of 4 (<= 8)
-    const int mlo = g * MRW, mhi = min(mlo + MRW, mcount);  // local m range of this warp
+    // this warp's m: pairs [pb0, pb1) of the block's ceil(mcount / 2) pairs, spread evenly
+    const int npairs = (mcount + 1) >> 1;
+    const int pb0 = (g * npairs) >> 4, pb1 = ((g + 1) * npairs) >> 4;
+    const int mlo = 2 * pb0, mhi = min(2 * pb1, mcount);  // local m range of this warp
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
     const size_t set = (size_t)stride * cat.lrows;
@@ -437,13 +456,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
             const float2 yu2 = make_float2(Y_UNSCALE, Y_UNSCALE);
 #pragma unroll
-            for (int gq = 0; gq < 2; ++gq) {
-                const int ml0 = mlo + 4 * gq;
-                if (ml0 < mhi) {
-                    float2 yr[2], yi[2];
-#pragma unroll
-                    for (int hp = 0; hp < 2; ++hp) {
-                        const int ml = ml0 + 2 * hp;  // even local m
+            for (int pp = 0; pp < 4; ++pp) {
+                const int ml = mlo + 2 * pp;  // even local m
+                if (ml < mhi) {
+                    float2 yr, yi;
+                    {
                         const int m = mb0 + ml;
                         float2 P;
                         if (!EXT && m + 1 <= l - 2 && ml + 1 < mcount) {
@@ -524,14 +541,14 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                             P = make_float2(pv[0], pv[1]);
                         }
                         const float2 Pu = __fmul2_rn(P, yu2);
-                        yr[hp] = __fmul2_rn(Pu, cm);
-                        yi[hp] = __fmul2_rn(Pu, nsm);
+                        yr = __fmul2_rn(Pu, cm);
+                        yi = __fmul2_rn(Pu, nsm);
                         // e^{i (m+2) phi} = e^{i m phi} e^{2 i phi}
                         const float2 cmn = __ffma2_rn(cm, c22, __fmul2_rn(nsm, s22));
                         nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
                         cm = cmn;
                     }
-                    store_split8p(yhi, ylo, tc05::mn_sw128_off(2 * ml0, q, 4), yr[0], yi[0], yr[1], yi[1]);
+                    store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
                 }
             }
         }

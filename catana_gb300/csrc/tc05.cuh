@@ -80,9 +80,20 @@ __device__ __forceinline__ uint64_t globaltimer() {
     return t;
 }
 
+// One non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_try(uint64_t *mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(smem_u32(mbar)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
 // Wait until the phase with the given parity completes, for at most limit_ns.
 // Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try(mbar, parity)) return true;
     const uint64_t t0 = globaltimer();
     while (true) {
         uint32_t done;
