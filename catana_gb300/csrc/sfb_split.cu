@@ -36,6 +36,8 @@
 // CTA generates tile t+1.  Every wait on an mbarrier is bounded (1 s); on timeout the
 // kernel records CATANA_ERR_CUDA in the error word, stops issuing work and frees its
 // tensor memory.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -112,6 +114,7 @@ struct SplitCat {
     int epitch;             // exponent words per tile (lrows rounded up to even)
     unsigned long long *rexp;  // extended range: three exponent sets [tile][lrows], set k at rexp + k * eset
     int64_t eset;           // words per exponent set
+    const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..2, then exponent words of sets 0..2
     const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
 };
@@ -205,7 +208,8 @@ template <bool EXT>
 __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t mbar[2];  // MMA completion per operand buffer
+    __shared__ uint64_t sbar[2];  // TMA completion per stage
     __shared__ uint32_t tmem_base_sh;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -249,6 +253,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     if (tid == 0) {
         tc05::mbar_init(&mbar[0], 1);
         tc05::mbar_init(&mbar[1], 1);
+        tc05::mbar_init(&sbar[0], 1);
+        tc05::mbar_init(&sbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tc05::tmem_alloc(&tmem_base_sh, tcols);
     tc05::fence_before();
@@ -279,6 +286,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     float *partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
+    uint32_t sfill0 = 0, sfill1 = 0, swait0 = 0, swait1 = 0;  // stage loads issued / waited
     bool acc_fresh = true;   // next fold overwrites D_acc
     bool first_flush = true; // partial rows not yet written by this CTA
     int folds = 0;
@@ -294,36 +302,48 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         return true;
     };
 
-    // stage the Legendre rows of tile t (this block's m) into stage buffer t&1
+    // stage tile t into stage t&1, all by one thread, completing on sbar[t&1]: the point
+    // records (one bulk copy), the rows P_{l-1}(m) and P_{l-2}(m) of this block's m in
+    // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
+    // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
+    // and (extended range) the exponent words of both sets
+    const char *tm_r1 = cat.tmaps + 128 * ((l + 2) % 3), *tm_r2 = cat.tmaps + 128 * ((l + 1) % 3);
+    const char *tm_e1 = cat.tmaps + 128 * (3 + (l + 2) % 3), *tm_e2 = cat.tmaps + 128 * (3 + (l + 1) % 3);
+    const int nb1 = l > 0 ? (mcount + 31) >> 5 : 0;
+    const int nb2 = (max(0, min(mcount, l - 1 - mb0)) + 31) >> 5;
+    const uint32_t stage_bytes =
+        SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? 2u * (MBLK * 8) : 0u);
+    if (tid == 0) {  // descriptors rewritten by the host between launches: read them afresh
+        tc05::tmap_acquire(tm_r1);
+        tc05::tmap_acquire(tm_r2);
+        if (EXT) {
+            tc05::tmap_acquire(tm_e1);
+            tc05::tmap_acquire(tm_e2);
+        }
+    }
     auto prefetch_rows = [&](int64_t t) {
         if (t >= t1) return;
-        uint8_t *stg = sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE;
-        const int64_t i0 = t * KT;
-        // the tile's point records (the buffer is padded to whole tiles)
-        if (tid < (int)(SM_STPTS / 16))
-            tc05::cp_async16(stg + 2 * SM_STROW + tid * 16,
-                             reinterpret_cast<const uint8_t *>(cat.pts + i0) + tid * 16);
-        if (l == 0) return;
-        if (EXT) {  // exponent words of the block's m (16-byte pieces; the sets carry a pad word)
-            const int ep = (mcount + 1) >> 1;
-            for (int c = tid; c < 2 * ep; c += NTHR) {
-                const int which = c >= ep;
-                const int pc = which ? c - ep : c;
-                const unsigned long long *src = (which ? ex2 : ex1) + t * cat.epitch + mb0 + 2 * pc;
-                tc05::cp_async16(stg + 2 * SM_STROW + SM_STPTS + which * MBLK * 8 + pc * 16, src);
-            }
+        const int sidx = (int)(t & 1);
+        if (sidx) ++sfill1; else ++sfill0;
+        if (tid != 0) return;
+        uint8_t *stg = sm + OFF_ST + (uint32_t)sidx * SM_STAGE;
+        tc05::fence_proxy_async();  // earlier generic reads of this stage before the async writes
+        tc05::mbar_arrive_expect_tx(&sbar[sidx], stage_bytes);
+        tc05::bulk_g2s(stg + 2 * SM_STROW, cat.pts + t * KT, SM_STPTS, &sbar[sidx]);
+        const int x = (int)(t * KT);
+        for (int k = 0; k < nb1; ++k) tc05::tma_load_2d(stg + k * 4096, tm_r1, x, mb0 + 32 * k, &sbar[sidx]);
+        for (int k = 0; k < nb2; ++k)
+            tc05::tma_load_2d(stg + SM_STROW + k * 4096, tm_r2, x, mb0 + 32 * k, &sbar[sidx]);
+        if (EXT && l > 0) {
+            tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
+            tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
         }
-        const int per_set = mcount * 8;  // 16-byte pieces per row set
-        for (int c = tid; c < 2 * per_set; c += NTHR) {
-            const int which = c >= per_set;
-            const int rem = which ? c - per_set : c;
-            const int ml = rem >> 3, part = rem & 7;
-            const int m = mb0 + ml;
-            if (which && m > l - 2) continue;
-            const int msrc = (m == l) ? l - 1 : m;
-            const float *src = (which ? st2 : st1) + (int64_t)msrc * stride + i0 + part * 4;
-            tc05::cp_async16(stg + which * SM_STROW + ml * 128 + part * 16, src);
-        }
+    };
+    auto wait_stage = [&](int sidx) -> bool {
+        uint32_t &sw = sidx ? swait1 : swait0;
+        if (!tc05::mbar_wait(&sbar[sidx], sw & 1u, WAIT_NS)) return false;
+        ++sw;
+        return true;
     };
 
     // D_acc (+)= D_tile, every warp: lane quadrant warp%4, column groups warp/4, +4, ...
@@ -381,18 +401,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     };
 
     prefetch_rows(t0);
-    tc05::cp_async_commit();
     for (int64_t t = t0; t < t1 && ok; ++t) {
         const int b = (int)((t - t0) & 1);
         prefetch_rows(t + 1);
-        tc05::cp_async_commit();
-        // operand buffer b is free once the MMAs of tile t-2 have completed
-        const int w_ok = wait_buf(b) ? 1 : 0;
-        tc05::cp_async_wait_prev();
-        if (!__syncthreads_and(w_ok)) {
-            ok = false;
-            break;
-        }
+        // operand buffer b is free once the MMAs of tile t-2 have completed, and tile t is
+        // staged; each thread waits for itself (a failed wait aborts at the barrier below)
+        int tok = (wait_buf(b) && wait_stage((int)(t & 1))) ? 1 : 0;
         uint8_t *bufp = sm + b * SM_BUF;
         uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
         const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
@@ -492,8 +506,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                                     } else {
                                         const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
                                         const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
-                                        const float p1 = stg1[mlh * KT + q];
                                         const bool sect = (mh == l);
+                                        const float p1 = stg1[(sect ? mlh - 1 : mlh) * KT + q];  // sectoral: P_{l-1,l-1}
                                         const float xa = sect ? sh : xh, xb = sect ? sl : xl;
                                         float p2 = (mh <= l - 2) ? stg2[mlh * KT + q] : 0.f;
                                         if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
@@ -555,18 +569,20 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         tc05::fence_proxy_async();
         // ---- every FOLD_TILES tiles: fold the tensor-core sum into D_acc (needs its MMAs complete) ----
         const bool fold_now = (t > t0) && ((t - t0) % FOLD_TILES == 0);
-        if (fold_now) {
+        if (fold_now) {  // each warp folds (and flushes) its own TMEM columns
             const int pb = b ^ 1;
-            const int f_ok = wait_buf(pb) ? 1 : 0;
-            if (!__syncthreads_and(f_ok)) {
-                ok = false;
-                break;
+            if (__all_sync(0xffffffffu, wait_buf(pb))) {
+                fold();
+                if (folds == FLUSH_FOLDS) flush();
+            } else {
+                tok = 0;
             }
-            fold();
-            if (folds == FLUSH_FOLDS) flush();
         }
         tc05::fence_before();
-        __syncthreads();
+        if (!__syncthreads_and(tok)) {
+            ok = false;
+            break;
+        }
         tc05::fence_after();
         // ---- hand tile t to the tensor cores: D_tile (+)= Jhi Yhi + Jhi Ylo + Jlo Yhi ----
         const bool fresh_tile = ((t - t0) % FOLD_TILES == 0);  // D_tile was folded (or never used)
@@ -603,7 +619,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         wait_buf(1);
         if (tid == 0) *a.err = CATANA_ERR_CUDA;
     }
-    tc05::cp_async_wait_all();
+    // stage loads still in flight (a loop that stopped early) land before the CTA exits
+    while (swait0 < sfill0 && wait_stage(0)) {
+    }
+    while (swait1 < sfill1 && wait_stage(1)) {
+    }
     // an empty slab still owns partial rows: write zeros so the reduction sees them
     if (t0 >= t1) {
         for (int t = tid; t < ncols * 128; t += NTHR) partial_cta[t] = 0.f;
@@ -879,6 +899,33 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
 // (16-byte copies of an odd m count read one word past the block)
 int64_t exp_set_words(const CatPlan &P) { return P.ntiles * ((P.in.lmax + 1) & ~1) + 2; }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D row-major tensor [d1][d0] at `base` (row pitch `pitch` bytes), box b0 x b1
+bool tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t d0, uint64_t d1, uint64_t pitch, uint32_t b0,
+             uint32_t b1) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {d0, d1};
+    const cuuint64_t strides[1] = {pitch};
+    const cuuint32_t box[2] = {b0, b1};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(m, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // autotune cache key: catalog count, sizes and multipoles of a group
 std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
     std::string k = std::to_string(c1 - c0);
@@ -1057,7 +1104,33 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             memcpy(host.data() + o, p, b);
             return o;
         };
-        std::vector<size_t> o_kz(gn), o_nl(gn);
+        std::vector<size_t> o_kz(gn), o_nl(gn), o_tm(gn);
+        for (int c = c0; c < c1; ++c) {
+            // TMA descriptors: the three Legendre row sets ([lmax][stride] FP32, 32 x 32 boxes)
+            // and, extended range, the three exponent sets ([tile][epitch] words, 128 x 1 boxes)
+            CatPlan &P = cats[c];
+            CUtensorMap tm[6];
+            memset(tm, 0, sizeof(tm));
+            char *rows = ws + off_rows[c - c0];
+            const size_t set_bytes = (size_t)P.stride * P.in.lmax * sizeof(float);
+            for (int k = 0; k < 3; ++k)
+                if (!tmap_2d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, (uint64_t)P.stride,
+                             (uint64_t)P.in.lmax, (uint64_t)P.stride * sizeof(float), 32, 32)) {
+                    set_error("cuTensorMapEncodeTiled failed for the Legendre rows");
+                    return CATANA_ERR_CUDA;
+                }
+            if (ext) {
+                const int ep = (P.in.lmax + 1) & ~1;
+                char *ex = ws + off_exp[c - c0];
+                for (int k = 0; k < 3; ++k)
+                    if (!tmap_2d(&tm[3 + k], CU_TENSOR_MAP_DATA_TYPE_UINT64, ex + (size_t)k * exp_set_words(P) * 8,
+                                 (uint64_t)ep, (uint64_t)P.ntiles, (uint64_t)ep * 8, 128, 1)) {
+                        set_error("cuTensorMapEncodeTiled failed for the row exponents");
+                        return CATANA_ERR_CUDA;
+                    }
+            }
+            o_tm[c - c0] = put(tm, sizeof(tm));
+        }
         for (int c = c0; c < c1; ++c) {
             CatPlan &P = cats[c];
             const int L = P.in.lmax, M = P.in.nmax;
@@ -1099,6 +1172,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.epitch = (P.in.lmax + 1) & ~1;
             sc.rexp = ext ? reinterpret_cast<unsigned long long *>(ws + off_exp[c - c0]) : nullptr;
             sc.eset = ext ? exp_set_words(P) : 0;
+            sc.tmaps = nullptr;  // patched at upload
             sc.kz = nullptr;  // patched below, once the plan buffer's address is known
             sc.nmax_l = nullptr;
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
@@ -1203,6 +1277,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             for (int c = c0; c < c1; ++c) {
                 SplitCat *sc = reinterpret_cast<SplitCat *>(host.data() + o_cats) + (c - c0);
                 sc->kz = reinterpret_cast<const float4 *>(pd + o_kz[c - c0]);
+                sc->tmaps = pd + o_tm[c - c0];
                 sc->nmax_l = reinterpret_cast<const int *>(pd + o_nl[c - c0]);
             }
             if (ib) memcpy(host.data() + o_items, S.items.data(), ib);

@@ -107,6 +107,38 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint6
     }
 }
 
+// One arrival that also announces `bytes` of asynchronous copies on this phase.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bulk copy global -> this CTA's shared memory (16-byte aligned, size a multiple of
+// 16); completion is counted in bytes on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void *dst_smem, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+// Make a TMA descriptor in global memory, written through the generic proxy (a host
+// copy), visible to the tensor-map proxy of this thread.
+__device__ __forceinline__ void tmap_acquire(const void *tmap) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+}
+
+// 2-D tiled TMA load of one box at element coordinates (x, y) of the tensor map at
+// `tmap` (global memory); completion is counted in bytes on the mbarrier.
+__device__ __forceinline__ void tma_load_2d(void *dst_smem, const void *tmap, int x, int y, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst_smem)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // 32 lanes x 16 consecutive 32-bit columns from TMEM (this warp's lane quadrant).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
