@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         ex2 = cat.rexp + (size_t)((l + 1) % 3) * cat.eset;
         ex0 = cat.rexp + (size_t)(l % 3) * cat.eset;
     }
-    float *partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
+    float *__restrict__ partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
     uint32_t sfill0 = 0, sfill1 = 0, swait0 = 0, swait1 = 0;  // stage loads issued / waited
@@ -383,15 +383,23 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             tc05::tmem_wait_ld();
             if (lane_n < nmax) {
                 const float inv_scale = s_inv[lane_n];
+                // all 16 reads of the running partial first (L2-resident), then the writes
+                float old[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int col = gi * 16 + j;
                     const int ml = col_m(col);
-                    if (ml < mcount) {
-                        const float d = __uint_as_float(v[j]) * inv_scale;
-                        float *p = partial_cta + (size_t)(2 * ml + col_ri(col)) * 128 + lane_n;
-                        *p = first_flush ? d : (*p + d);
-                    }
+                    old[j] = (!first_flush && ml < mcount)
+                                 ? __ldcg(partial_cta + (size_t)(2 * ml + col_ri(col)) * 128 + lane_n)
+                                 : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = gi * 16 + j;
+                    const int ml = col_m(col);
+                    if (ml < mcount)
+                        __stcg(partial_cta + (size_t)(2 * ml + col_ri(col)) * 128 + lane_n,
+                               __uint_as_float(v[j]) * inv_scale + old[j]);
                 }
             }
         }
