@@ -467,16 +467,19 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
         if (mlo < mhi) {
             const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
-            // e^{i m phi} for the pair (m, m+1): seed m, one rotation by e^{i phi}; pairs then
-            // advance by e^{2 i phi}.  nsm holds -sin.
+            // e^{i m phi} for the pair (m, m+1), times the readout factor 2^-88 of the scaled
+            // rows (exact): seed m, one rotation by e^{i phi}; pairs then advance by
+            // e^{2 i phi}.  nsm holds -sin.
             float cma, sma;
             phase_seed(pt.u, mb0 + mlo, cma, sma);
+            cma *= Y_UNSCALE;
+            sma *= Y_UNSCALE;
             float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
             float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
+            float *rowp = st0 + (int64_t)(mb0 + mlo) * stride + i;  // P_l row of the pair's first m
             const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
             const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
             const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
-            const float2 yu2 = make_float2(Y_UNSCALE, Y_UNSCALE);
 #pragma unroll
             for (int pp = 0; pp < 4; ++pp) {
                 const int ml = mlo + 2 * pp;  // even local m
@@ -496,8 +499,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                             const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
                             P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
                             if (wrows) {
-                                st0[(int64_t)m * stride + i] = P.x;
-                                st0[(int64_t)(m + 1) * stride + i] = P.y;
+                                rowp[0] = P.x;
+                                rowp[stride] = P.y;
                             }
                         } else {
                             // sectoral (m = l), m = l - 1, the block's last odd m, or extended range
@@ -550,7 +553,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                                             }
                                         }
                                     }
-                                    if (wrows) st0[(int64_t)mh * stride + i] = Pq;
+                                    if (wrows) rowp[h ? stride : 0] = Pq;
                                     if (EXT && wrows) {
                                         const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
                                         const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
@@ -562,9 +565,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                             }
                             P = make_float2(pv[0], pv[1]);
                         }
-                        const float2 Pu = __fmul2_rn(P, yu2);
-                        yr = __fmul2_rn(Pu, cm);
-                        yi = __fmul2_rn(Pu, nsm);
+                        yr = __fmul2_rn(P, cm);
+                        yi = __fmul2_rn(P, nsm);
                         // e^{i (m+2) phi} = e^{i m phi} e^{2 i phi}
                         const float2 cmn = __ffma2_rn(cm, c22, __fmul2_rn(nsm, s22));
                         nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
@@ -572,6 +574,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                     }
                     store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
                 }
+                rowp += 2 * (int64_t)stride;
             }
         }
         tc05::fence_proxy_async();
