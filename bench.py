@@ -517,14 +517,14 @@ def main():
         kernel = "k_fp64_raw_l"
     achieved = (kfl.value / (kms.value / 1e3)) / 1e12 if kms.value > 0 else None
     # DRAM bytes of an average k_split_l launch: the ncu capture of l = 200 on 300k points
-    # (profiles/k_split_l_l200_300k_full.md) read+wrote 808 MB = 1.09 x the algorithmic
-    # 12 B per (point, m) of Legendre rows + 48 B per point; scaled here to this run's
-    # chunk size and averaged over l.
+    # (profiles/k_split_l_l200_300k_full.md) read+wrote 847 MB = 1.15 x the algorithmic
+    # 12 B per (point, m) of Legendre rows + 48 B per point (738 MB); scaled here to this
+    # run's chunk size and averaged over l.
     traffic = None
     if a.form == "split":
         chunk = min(a.points, int(16e9 / (12.0 * L)))
         avg = sum((12.0 * (l + 1) + 48.0) * chunk for l in range(L)) / L
-        traffic = 1.09 * avg
+        traffic = 1.15 * avg
     roof = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
             "traffic_unit": "bytes per launch (average over l), from one ncu capture scaled by points",
