@@ -11,9 +11,9 @@ from . import _lib  # noqa: F401  (raises ImportError when the library is missin
 from . import besseltools
 from .basictypes import PixelizedPointContainer, Point, PointContainer
 from .decomposition import (KClkk, SFBAccumulator, compute_kln, sfb_decomposition, sfb_decomposition_batched,
-                            sfb_decomposition_healpix)
+                            sfb_decomposition_healpix, sfb_reverse)
 
 __all__ = ["Point", "PointContainer", "PixelizedPointContainer", "KClkk", "sfb_decomposition",
-           "sfb_decomposition_healpix", "sfb_decomposition_batched", "SFBAccumulator", "compute_kln",
+           "sfb_decomposition_healpix", "sfb_decomposition_batched", "SFBAccumulator", "sfb_reverse", "compute_kln",
            "besseltools"]
 __version__ = "0.1.0"

@@ -54,6 +54,7 @@ SIGNATURES = {
     "catana_gpu_accum_finish": (ctypes.c_int, [_P, _P, _P, _P]),
     "catana_gpu_accum_destroy": (ctypes.c_int, [_P]),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
+    "catana_gpu_sfb_reverse": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_bin_points": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
     "catana_gpu_ang2pix_ring": (ctypes.c_int, [_I64, _P, _P, _I64, _P, _P]),
     "catana_gpu_pix2ang_ring": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),

@@ -709,6 +709,17 @@ catana_status_t catana_gpu_pix2ang_ring(int64_t nside, const int64_t *pix, int64
     return CATANA_OK;
 }
 
+catana_status_t catana_gpu_sfb_reverse(int64_t nside, const int64_t *pix_offsets, const double *r_sorted,
+                                       uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags, double *k_ln,
+                                       double *c_ln, double *f_lmn, catana_gpu_stream_t stream) {
+    // _sfb_reverse's dense sum over pixels, f(m, n) = sum_pix Y_lm(pix) map(pix, n), splits
+    // over rings: a ring's pixels share theta and have equally spaced phi, so its part is
+    // P_lm(theta_ring) e^{-i m phi_0} times the ring DFT of the map at m mod rpix -- read as
+    // the conjugate of F[rpix - m mod rpix] past rpix/2 (the corrected alias).
+    return catana_gpu_sfb_healpix(nside, pix_offsets, r_sorted, lmax, nmax, rmax, flags | CATANA_HEALPIX_CONJ_FIX,
+                                  k_ln, c_ln, f_lmn, stream);
+}
+
 catana_status_t catana_gpu_bin_points(int64_t nside, const double *points, int64_t npoints, int64_t *pix_offsets,
                                       double *r_sorted, catana_gpu_stream_t stream) {
     if (nside < 1 || (nside & (nside - 1)) != 0) {

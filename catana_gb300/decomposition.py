@@ -147,6 +147,30 @@ def sfb_decomposition(point_container, lmax, nmax, rmax, store_flmn=False, verbo
     return _raw(point_container, lmax, nmax, rmax, store_flmn, verbose, weights, precision, interpolation)
 
 
+def sfb_reverse(pixelized_point_container, lmax, nmax, rmax, store_flmn=False, verbose=True, interpolated=True):
+    """The pixelized SFB without FFT, the reference's _sfb_reverse (sfb_reverse.cpp:13-112):
+    per l, f = Y*_lm(pixel centres) x (per-pixel sums of j_l(k_ln r)).  `interpolated`
+    picks the j_l branch as in that function.  Returns a KClkk."""
+    ppc = pixelized_point_container
+    if not isinstance(ppc, PixelizedPointContainer):
+        raise TypeError("sfb_reverse expects a PixelizedPointContainer")
+    lmax = _unsigned_short(lmax, "lmax")
+    nmax = _unsigned_short(nmax, "nmax")
+    if verbose:
+        print("SFB decomposition (reverse method): lmax=%d nmax=%d NSide=%d" % (lmax, nmax, ppc.nside))
+        print("Catalog consists of %d points." % ppc.get_npoints())
+        sys.stdout.flush()
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    f = np.zeros(int(_lib.lib.catana_gpu_flmn_size(lmax, nmax)), dtype=np.complex128) if store_flmn else None
+    rs = ppc.r_sorted if ppc.r_sorted.size else np.zeros(1)
+    flags = _lib.JL_INTERP if interpolated else _lib.JL_EXACT
+    st = _lib.lib.catana_gpu_sfb_reverse(ppc.nside, _lib.ptr(ppc.offsets), _lib.ptr(rs), lmax, nmax, float(rmax),
+                                         flags, _lib.ptr(k), _lib.ptr(c), _lib.ptr(f), None)
+    _lib.check(st, "sfb_reverse")
+    return KClkk(k, c, unpack_flmn(f, lmax, nmax) if store_flmn else [])
+
+
 def sfb_decomposition_healpix(pixelized_point_container, lmax, nmax, rmax, store_flmn=False, verbose=True,
                               interpolation="auto", conj_fix=False):
     """Alias of sfb_decomposition for a PixelizedPointContainer."""

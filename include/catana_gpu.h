@@ -197,6 +197,16 @@ catana_status_t catana_gpu_sfb_healpix(int64_t nside, const int64_t *pix_offsets
                                        uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags, double *k_ln,
                                        double *c_ln, double *f_lmn, catana_gpu_stream_t stream);
 
+/* Pixelized SFB without FFT: the reference's _sfb_reverse (sfb_reverse.cpp:13-112),
+ * which the public wrappers do not call.  Same arguments and outputs as
+ * catana_gpu_sfb_healpix; f_lmn = sum over pixels of Y*_lm(pixel centre) times the
+ * pixel's sum of j_l(k_ln r), with the C_ln and f normalisation of that file.  The
+ * JL flag picks the j_l branch (the reference passes `interpolated` explicitly;
+ * CATANA_JL_AUTO applies the N > 1000 rule). */
+catana_status_t catana_gpu_sfb_reverse(int64_t nside, const int64_t *pix_offsets, const double *r_sorted,
+                                       uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags, double *k_ln,
+                                       double *c_ln, double *f_lmn, catana_gpu_stream_t stream);
+
 /* Bin a catalog into RING pixels: the PixelizedPointContainer(nside, pc)
  * constructor (PixelizedPointContainer.cpp:11-30).  points: host npoints x 3
  * (r, theta, phi).  Outputs (host): pix_offsets[npix+1] and r_sorted[npoints],

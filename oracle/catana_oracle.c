@@ -629,6 +629,102 @@ int co_sfb_healpix(int64_t nside, const int64_t *offsets, const double *r_sorted
     return err_any ? 2 : 0;
 }
 
+/* _sfb_reverse (sfb_reverse.cpp:13-112): per l, Y(m, pix) = sphPlm(l, m, cos theta_pix)
+ * e^{-i m phi_pix} at every pixel centre (:63-70), map(pix, n) = sum over the pixel's
+ * radii of j_l(k_ln r) (:73-81), f_l = Y map (:88), C_ln = sum_{m=-l..l} |f_l|m|n|^2
+ * (norm k)^2 / (2l+1) (:91-96), stored f = f k norm (:98-102); norm = sqrt(2/pi) 4/3 pi
+ * rmax^3 / N (:29-30).  Interpolation as the raw path (:44-51). */
+int co_sfb_reverse(int64_t nside, const int64_t *offsets, const double *r_sorted, int lmax, int nmax, double rmax,
+                   int interpolated, int nthreads, double *k_ln, double *c_ln, double *f_re, double *f_im)
+{
+    if (!f_re || !f_im) return 3; /* f is needed for C_ln; callers always pass it */
+    if (nthreads <= 0) {
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#else
+        nthreads = 1;
+#endif
+    }
+    int64_t npix = 12 * nside * nside;
+    int64_t npoints = offsets[npix];
+    double norm_factor = sqrt(2. / CO_PI) * (4. / 3.) * CO_PI;
+    norm_factor *= rmax * rmax * rmax / (double)npoints;
+    co_compute_kln(lmax, nmax, rmax, k_ln);
+    memset(c_ln, 0, sizeof(double) * (size_t)lmax * nmax);
+    double *th = (double *)malloc(sizeof(double) * npix);
+    double *ph = (double *)malloc(sizeof(double) * npix);
+    for (int64_t p = 0; p < npix; ++p) co_pix2ang_ring(nside, p, &th[p], &ph[p]);
+    int npts_tab = 1000 * nmax;
+    double *table = interpolated ? (double *)malloc(sizeof(double) * npts_tab) : NULL;
+    double *zl = (double *)malloc(sizeof(double) * (nmax + 1 > 2 ? nmax + 1 : 2));
+    double *map = (double *)malloc(sizeof(double) * (size_t)npix * (nmax > 0 ? nmax : 1));
+    int err_any = 0;
+    size_t foff = 0;
+    for (int l = 0; l < lmax; ++l) {
+        double dx_inv = 0.0, zmax = 0.0;
+        if (interpolated) {
+            co_sbessel_zeros((unsigned)l, nmax + 1, zl);
+            zmax = zl[nmax];
+            co_lerp_table(l, zmax, npts_tab, table, &dx_inv);
+        }
+#pragma omp parallel for num_threads(nthreads) reduction(| : err_any) schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            int err = 0;
+            for (int n = 0; n < nmax; ++n) {
+                double k_n = k_ln[(size_t)l * nmax + n], s = 0.0;
+                for (int64_t q = offsets[p]; q < offsets[p + 1]; ++q) {
+                    double z = k_n * r_sorted[q];
+                    s += interpolated ? co_lerp_eval(table, npts_tab, dx_inv, zmax, z, &err) : co_sbessel_jl(l, z);
+                }
+                map[(size_t)p * nmax + n] = s;
+            }
+            err_any |= err;
+        }
+        /* f(m, n) = sum_pix Y(m, pix) map(pix, n), pixels in order */
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+        for (int m = 0; m <= l; ++m) {
+            double *fr = (double *)calloc((size_t)nmax, sizeof(double));
+            double *fi = (double *)calloc((size_t)nmax, sizeof(double));
+            for (int64_t p = 0; p < npix; ++p) {
+                double pl = co_sph_plm(l, m, cos(th[p]));
+                double yr = pl * cos(-m * ph[p]), yi = pl * sin(-m * ph[p]);
+                for (int n = 0; n < nmax; ++n) {
+                    double v = map[(size_t)p * nmax + n];
+                    fr[n] += yr * v;
+                    fi[n] += yi * v;
+                }
+            }
+            for (int n = 0; n < nmax; ++n) {
+                size_t o = foff + (size_t)m * nmax + n;
+                f_re[o] = fr[n];
+                f_im[o] = fi[n];
+            }
+            free(fr);
+            free(fi);
+        }
+        for (int n = 0; n < nmax; ++n) {
+            double kk = k_ln[(size_t)l * nmax + n], c = 0.0;
+            for (int m = -l; m <= l; ++m) {
+                size_t o = foff + (size_t)(m < 0 ? -m : m) * nmax + n;
+                c += f_re[o] * f_re[o] + f_im[o] * f_im[o];
+            }
+            c_ln[(size_t)l * nmax + n] = c * pow(norm_factor * kk, 2) / (2 * l + 1);
+            for (int m = 0; m <= l; ++m) {
+                size_t o = foff + (size_t)m * nmax + n;
+                f_re[o] *= kk * norm_factor;
+                f_im[o] *= kk * norm_factor;
+            }
+        }
+        foff += (size_t)(l + 1) * nmax;
+    }
+    free(th);
+    free(ph);
+    free(table);
+    free(zl);
+    free(map);
+    return err_any ? 2 : 0;
+}
+
 /* Point(x, y, z): Point.cpp:5-10 -- r = |v|, theta = atan2(rho, z),
  * phi = atan2(y, x) reduced into [0, 2 pi) (HEALPix pointing(vec3) + normalize). */
 void co_cartesian_to_spherical(const double *xyz, int64_t n, double *rtp)

@@ -69,6 +69,8 @@ def lib():
         L.co_bin_points.argtypes = [_I64, _P, _I64, _P, _P]
         L.co_sfb_healpix.restype = _I
         L.co_sfb_healpix.argtypes = [_I64, _P, _P, _I, _I, _D, _I, _I, _P, _P, _P, _P]
+        L.co_sfb_reverse.restype = _I
+        L.co_sfb_reverse.argtypes = [_I64, _P, _P, _I, _I, _D, _I, _I, _P, _P, _P, _P]
         L.co_cartesian_to_spherical.restype = None
         L.co_cartesian_to_spherical.argtypes = [_P, _I64, _P]
         _lib = L
@@ -194,6 +196,22 @@ def bin_points(nside, pts):
     if rc != 0:
         raise ValueError("theta outside [0, pi]")
     return offs, rs[:pts.shape[0]]
+
+
+def sfb_reverse(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, nthreads=0):
+    """Pixelized SFB without FFT: dense Y(m, pixel) x map(pixel, n) per l (sfb_reverse.cpp:13-112)."""
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    r_sorted = np.ascontiguousarray(r_sorted, dtype=np.float64)
+    k = np.zeros((lmax, nmax))
+    c = np.zeros((lmax, nmax))
+    nf = nmax * lmax * (lmax + 1) // 2
+    fre = np.zeros(max(nf, 1))
+    fim = np.zeros(max(nf, 1))
+    rc = lib().co_sfb_reverse(int(nside), _ptr(offsets), _ptr(r_sorted), int(lmax), int(nmax), float(rmax),
+                              int(bool(interpolated)), int(nthreads), _ptr(k), _ptr(c), _ptr(fre), _ptr(fim))
+    if rc == 2:
+        raise ValueError("argument (z) outside of defined range.")
+    return k, c, _unpack_f(fre, fim, lmax, nmax)
 
 
 def sfb_healpix(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, store_flmn=True, nthreads=0):

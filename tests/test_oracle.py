@@ -147,3 +147,32 @@ def test_oracle_weights_reduce_to_unweighted():
     # doubling every weight changes nothing (normalised by the weight sum)
     k3, c3, f3 = O.sfb_raw(pts, 6, 5, 100.0, interpolated=False, weights=2 * np.ones(300))
     assert np.allclose(c1, c3, rtol=1e-13)
+
+
+def test_golden_reverse(golden):
+    """sfb_test.cpp:101-133: _sfb_reverse (nside 64, lmax = nmax = 10, rmax 2500; exact
+    and interpolated j_l) against the golden raw C_ln at the test's 10% bar, tightened:
+    within 1e-5 of the pixelized golden file (the same pixel sums; this catalog has no
+    ring where the FFT method's unconjugated alias matters at l < 10)."""
+    pts = O.cartesian_to_spherical(golden["xyz"])
+    offs, rs = O.bin_points(64, pts)
+    for interp in (False, True):
+        k, c, _ = O.sfb_reverse(64, offs, rs, 10, 10, 2500, interpolated=interp)
+        cc = c * golden["correction_factor"] ** 2
+        assert np.allclose(cc, golden["c_ln"], rtol=1e-1)
+        assert np.allclose(k, golden["k_ln_rev"])
+    k, c, _ = O.sfb_reverse(64, offs, rs, 10, 10, 2500, interpolated=False)
+    assert np.max(np.abs(c * golden["correction_factor"] ** 2 / golden["c_ln_rev"] - 1)) < 1e-5
+
+
+def test_reverse_equals_fft_path_away_from_aliasing():
+    """_sfb_reverse and _sfb_reverse_fft sum the same pixel maps; at l = 0, 1 no m
+    exceeds half of any ring's length (the shortest ring has 4 pixels), so the FFT
+    method's unconjugated alias does not enter and the two agree to rounding."""
+    pts = uniform_ball(4000, 300.0, seed=17)
+    offs, rs = O.bin_points(16, pts)
+    k1, c1, f1 = O.sfb_reverse(16, offs, rs, 8, 6, 300.0, interpolated=False)
+    k2, c2, f2 = O.sfb_healpix(16, offs, rs, 8, 6, 300.0, interpolated=False)
+    # l = 0, 1: every ring has >= 4 pixels > 2 l, no alias
+    for l in (0, 1):
+        assert np.max(np.abs(f1[l] - f2[l])) <= 1e-12 * np.max(np.abs(f2[l]))
