@@ -40,6 +40,18 @@ class Catalog(ctypes.Structure):
                 ("c_ln", ctypes.c_void_p), ("f_lmn", ctypes.c_void_p), ("lmax", ctypes.c_uint16),
                 ("nmax", ctypes.c_uint16), ("reserved", ctypes.c_uint32)]
 
+REC_FLOAT64, REC_FLOAT32 = 0, 1
+REC_SPHERICAL, REC_CARTESIAN = 0, 2
+
+
+class IngestSpec(ctypes.Structure):
+    """catana_ingest_t: record layout and point filters for the device ingest."""
+    _fields_ = [("layout", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("tophat_r0", ctypes.c_double),
+                ("gauss_r0", ctypes.c_double), ("window", ctypes.c_void_p), ("window_n", ctypes.c_int64),
+                ("window_min", ctypes.c_double), ("window_max", ctypes.c_double), ("mask", ctypes.c_void_p),
+                ("mask_nside", ctypes.c_int64), ("seed", ctypes.c_uint64), ("index0", ctypes.c_uint64)]
+
+
 SIGNATURES = {
     "catana_gpu_flmn_size": (ctypes.c_size_t, [_U16, _U16]),
     "catana_gpu_sfb_raw": (ctypes.c_int, [_P, _P, _I64, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
@@ -52,6 +64,8 @@ SIGNATURES = {
     "catana_gpu_accum_add_f32": (ctypes.c_int, [_P, _P, _P, _I64]),
     "catana_gpu_accum_add": (ctypes.c_int, [_P, _P, _P, _I64]),
     "catana_gpu_accum_finish": (ctypes.c_int, [_P, _P, _P, _P]),
+    "catana_gpu_accum_add_records": (ctypes.c_int, [_P, _P, _I64, _P]),
+    "catana_gpu_ingest": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P]),
     "catana_gpu_accum_destroy": (ctypes.c_int, [_P]),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),
     "catana_gpu_sfb_reverse": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),

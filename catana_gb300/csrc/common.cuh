@@ -81,6 +81,7 @@ struct DeviceContext {
     cudaStream_t capture_stream = nullptr;      // stream the split level loop is captured on
     cudaEvent_t split_ws_event = nullptr;       // end of the last split run (orders workspace reuse across streams)
     DevBuf hp_ws;      // HEALPix workspace
+    DevBuf ingest_ws;  // ingest: converted records, keep flags, block counts, window, mask
     // cache keys
     int coef_lmax = -1;
     int tab_lmax = -1, tab_nmax = -1;
@@ -137,6 +138,10 @@ struct SplitCatInput {
 // items are cut for; <= 0 autotunes it (timed sample levels, cached per catalog set).
 catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats, bool use_graph, double waves,
                           int *err_dev, cudaStream_t st);
+
+// Convert, filter and compact n device records (ingest.cu); *n_out kept, in order.
+catana_status_t ingest_dev(DeviceContext *ctx, const void *rec_dev, int64_t n, const catana_ingest_t &spec,
+                           double *out_dev, int64_t *n_out, cudaStream_t st);
 
 // Split (tensor-core) raw path (sfb_split.cu).
 catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,

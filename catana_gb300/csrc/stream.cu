@@ -173,6 +173,72 @@ catana_status_t accum_add(Accum *A, const T *points, const T *weights, int64_t n
     return CATANA_OK;
 }
 
+// one chunk of raw records: stage in slot `k`, convert + filter + compact into slot64[k],
+// decompose the kept points
+catana_status_t accum_add_records(Accum *A, const void *records, int64_t n, const catana_ingest_t &spec) {
+    if (n < 0 || (n > 0 && !records)) {
+        set_error("n must be >= 0 and records non-null");
+        return CATANA_ERR_ARG;
+    }
+    if (A->finished) {
+        set_error("the accumulation is finished");
+        return CATANA_ERR_ARG;
+    }
+    if (A->weighted) {
+        set_error("all chunks of an accumulation must either carry weights or not");
+        return CATANA_ERR_ARG;
+    }
+    if (n == 0) return CATANA_OK;
+    A->unweighted = true;
+    DeviceContext *ctx = A->ctx;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    const int k = A->next;
+    A->next ^= 1;
+    const size_t rb = (size_t)n * 3 * ((spec.layout & CATANA_REC_FLOAT32) ? 4 : 8);
+    CG_CUDA_TRY(cudaEventSynchronize(A->consumed[k]));
+    CG_CUDA_TRY(A->slot[k].ensure(rb + 256));
+    CG_CUDA_TRY(A->slot64[k].ensure((size_t)n * 3 * sizeof(double) + 256));
+    CG_CUDA_TRY(cudaMemcpyAsync(A->slot[k].ptr, records, rb, cudaMemcpyHostToDevice, A->copy_st));
+    CG_CUDA_TRY(cudaEventRecord(A->copied[k], A->copy_st));
+    CG_CUDA_TRY(cudaStreamWaitEvent(A->comp_st, A->copied[k], 0));
+    int64_t kept = 0;
+    double *pts = A->slot64[k].as<double>();
+    catana_status_t s = ingest_dev(ctx, A->slot[k].ptr, n, spec, pts, &kept, A->comp_st);
+    if (s != CATANA_OK) return s;
+    int *err_d = A->err.as<int>();
+    if (kept > 0) {
+        if (A->split) {
+            if (ctx->cc_major != 10 || ctx->cc_minor != 3) {
+                set_error("the split (tcgen05) form needs an sm_103 device");
+                return CATANA_ERR_UNSUPPORTED;
+            }
+            const int64_t piece = std::max<int64_t>(
+                32, std::min<int64_t>(kept, (int64_t)(24e9 / ((A->lmax > 256 ? 15.0 : 12.0) * A->lmax))));
+            std::vector<SplitCatInput> v;
+            for (int64_t p0 = 0; p0 < kept; p0 += piece) {
+                SplitCatInput in;
+                in.pts = pts + 3 * p0;
+                in.n = std::min(piece, kept - p0);
+                in.lmax = A->lmax;
+                in.nmax = A->nmax;
+                in.rmax = A->rmax;
+                in.kln_dev = A->kln.as<double>();
+                in.f_acc = A->facc.as<double>();
+                v.push_back(in);
+            }
+            s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);
+        } else {
+            const uint32_t jl = A->flags & CATANA_JL_MASK;
+            s = fp64_raw_accumulate(ctx, pts, nullptr, kept, A->lmax, A->nmax, jl != CATANA_JL_EXACT,
+                                    A->kln.as<double>(), A->facc.as<double>(), err_d, A->comp_st);
+        }
+        if (s != CATANA_OK) return s;
+    }
+    CG_CUDA_TRY(cudaEventRecord(A->consumed[k], A->comp_st));
+    A->npoints += kept;
+    return CATANA_OK;
+}
+
 }  // namespace
 
 }  // namespace catana_gpu
@@ -247,6 +313,15 @@ catana_status_t catana_gpu_accum_add(catana_gpu_accum_t acc, const double *point
         return CATANA_ERR_ARG;
     }
     return accum_add<double>(reinterpret_cast<Accum *>(acc), points, weights, n);
+}
+
+catana_status_t catana_gpu_accum_add_records(catana_gpu_accum_t acc, const void *records, int64_t n,
+                                             const catana_ingest_t *spec) {
+    if (!acc || !spec) {
+        set_error("null accumulator or spec");
+        return CATANA_ERR_ARG;
+    }
+    return accum_add_records(reinterpret_cast<Accum *>(acc), records, n, *spec);
 }
 
 catana_status_t catana_gpu_accum_finish(catana_gpu_accum_t acc, double *k_ln, double *c_ln, double *f_lmn) {

@@ -240,6 +240,52 @@ def sfb_decomposition_batched(point_containers, lmax, nmax, rmax, kmax=None, wei
             for i, (k, c, f) in enumerate(out)]
 
 
+def _ingest_spec(records, coordinate_type, tophat_r0, gauss_r0, window, window_range, mask, seed, index0):
+    rec = np.asarray(records)
+    f32 = rec.dtype == np.float32
+    rec = np.ascontiguousarray(rec, dtype=np.float32 if f32 else np.float64).reshape(-1, 3)
+    if coordinate_type not in ("spherical", "cartesian"):
+        raise RuntimeError("coord_type either 'cartesian' or 'spherical'")
+    sp = _lib.IngestSpec()
+    sp.layout = (_lib.REC_FLOAT32 if f32 else _lib.REC_FLOAT64) | \
+        (_lib.REC_CARTESIAN if coordinate_type == "cartesian" else _lib.REC_SPHERICAL)
+    sp.tophat_r0 = float(tophat_r0 or 0.0)
+    sp.gauss_r0 = float(gauss_r0 or 0.0)
+    keep = [rec]
+    if window is not None:
+        w = np.ascontiguousarray(window, dtype=np.float64)
+        keep.append(w)
+        sp.window, sp.window_n = w.ctypes.data, w.size
+        sp.window_min, sp.window_max = float(window_range[0]), float(window_range[1])
+    if mask is not None:
+        m = np.ascontiguousarray(mask, dtype=np.float32)
+        nside = int(round(np.sqrt(m.size / 12)))
+        if 12 * nside * nside != m.size:
+            raise RuntimeError("healpix_map is not a valid map (check size!)")
+        keep.append(m)
+        sp.mask, sp.mask_nside = m.ctypes.data, nside
+    sp.seed, sp.index0 = int(seed), int(index0)
+    return rec, sp, keep
+
+
+def ingest(records, coordinate_type="spherical", tophat_r0=None, gauss_r0=None, window=None, window_range=(0.0, 1.0),
+           mask=None, seed=0, index0=0):
+    """Convert and filter a block of records on the GPU (no counterpart in the reference's
+    Python API; the filters are its TophatRadialWindowFunctionFilter,
+    GaussianRadialWindowFunctionFilter, GenericRadialWindowFunctionFilter with an
+    interpolated window, and AngularMaskFilter).  records: (N, 3) float32 or float64,
+    (x, y, z) or (r, theta, phi).  Random windows keep record i when w(r) > u_i with u_i
+    a hash of (seed, index0 + i).  Returns a PointContainer of the kept points, in order."""
+    rec, sp, keep = _ingest_spec(records, coordinate_type, tophat_r0, gauss_r0, window, window_range, mask, seed,
+                                 index0)
+    n = rec.shape[0]
+    out = np.zeros((max(n, 1), 3))
+    nout = ctypes.c_int64(0)
+    _lib.check(_lib.lib.catana_gpu_ingest(_lib.ptr(rec), n, ctypes.byref(sp), _lib.ptr(out), ctypes.byref(nout), None),
+               "ingest")
+    return PointContainer(out[:nout.value])
+
+
 class SFBAccumulator(object):
     """Raw SFB decomposition of one catalog fed in chunks (no counterpart in the
     reference).  ``add(points, weights=None)`` takes an (N, 3) array of (r, theta,
@@ -276,6 +322,19 @@ class SFBAccumulator(object):
         fn = _lib.lib.catana_gpu_accum_add_f32 if f32 else _lib.lib.catana_gpu_accum_add
         _lib.check(fn(self._h, _lib.ptr(pts), _lib.ptr(w), pts.shape[0]), "accum_add")
         self._keep = (self._keep + [(pts, w)])[-2:]
+
+    def add_records(self, records, coordinate_type="spherical", tophat_r0=None, gauss_r0=None, window=None,
+                    window_range=(0.0, 1.0), mask=None, seed=0, index0=None):
+        """Add a chunk of raw records, converted and filtered on the GPU as ``ingest``
+        does; index0 defaults to the number of records added so far."""
+        if index0 is None:
+            index0 = getattr(self, "_records_seen", 0)
+        rec, sp, keep = _ingest_spec(records, coordinate_type, tophat_r0, gauss_r0, window, window_range, mask, seed,
+                                     index0)
+        _lib.check(_lib.lib.catana_gpu_accum_add_records(self._h, _lib.ptr(rec), rec.shape[0], ctypes.byref(sp)),
+                   "accum_add_records")
+        self._records_seen = int(index0) + rec.shape[0]
+        self._keep = (self._keep + [tuple(keep)])[-2:]
 
     def finish(self, store_flmn=False):
         k = np.zeros((self.lmax, self.nmax))

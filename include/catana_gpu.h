@@ -176,6 +176,7 @@ double catana_gpu_batch_waves(void);
  * all carry weights or none.  finish() ends the accumulation.  An accumulator is
  * used from one thread at a time. */
 typedef struct catana_gpu_accum *catana_gpu_accum_t;
+typedef struct catana_ingest catana_ingest_t;  /* record layout and filters, defined below */
 catana_status_t catana_gpu_accum_create(uint16_t lmax, uint16_t nmax, double rmax, uint32_t flags,
                                         catana_gpu_accum_t *out);
 /* chunk of n float32 (r, theta, phi) records (the SphericalRecord<float> layout that
@@ -185,8 +186,48 @@ catana_status_t catana_gpu_accum_add_f32(catana_gpu_accum_t acc, const float *po
 /* chunk of n float64 (r, theta, phi) records and optional weights */
 catana_status_t catana_gpu_accum_add(catana_gpu_accum_t acc, const double *points, const double *weights,
                                      int64_t n);
+/* chunk of n raw records converted and filtered on the device (catana_ingest_t;
+ * index0 counts records across chunks for the random windows), the kept points
+ * decomposed; no weights */
+catana_status_t catana_gpu_accum_add_records(catana_gpu_accum_t acc, const void *records, int64_t n,
+                                             const catana_ingest_t *spec);
 catana_status_t catana_gpu_accum_finish(catana_gpu_accum_t acc, double *k_ln, double *c_ln, double *f_lmn);
 catana_status_t catana_gpu_accum_destroy(catana_gpu_accum_t acc);
+
+/* ---- catalog ingest on the device (no counterpart in the reference's API) ----
+ * Record conversion and the reference's point filters, run on the GPU ahead of a
+ * decomposition: the parts of its FilterStream pipeline (FilterStream.cpp:100-124)
+ * that touch every point. */
+#define CATANA_REC_FLOAT64 0u    /* records are 3 doubles */
+#define CATANA_REC_FLOAT32 1u    /* records are 3 floats (RawBinarySource<...Record<float>>) */
+#define CATANA_REC_SPHERICAL 0u  /* (r, theta, phi), taken as given (Point.cpp:23-28) */
+#define CATANA_REC_CARTESIAN 2u  /* (x, y, z) -> Point(x, y, z) (Point.cpp:5-10) */
+
+struct catana_ingest {
+    uint32_t layout;        /* CATANA_REC_* */
+    uint32_t reserved;      /* 0 */
+    double tophat_r0;       /* > 0: TophatRadialWindowFunctionFilter: keep r < R0 (radial_filters.cpp:32-34) */
+    double gauss_r0;        /* > 0: GaussianRadialWindowFunctionFilter: keep if exp(-(r/R0)^2) > u (:26-28) */
+    const double *window;   /* GenericRadialWindowFunctionFilter with an interpolated window: keep if w(r) > u;
+                               w on window_n equally spaced nodes of [window_min, window_max], evaluated as
+                               FunctionInterpolator (FunctionInterpolator.cpp:6-30; r outside -> CATANA_ERR_DOMAIN);
+                               host array, NULL = off */
+    int64_t window_n;
+    double window_min, window_max;
+    const float *mask;      /* AngularMaskFilter: RING map of 12 mask_nside^2 floats, keep if map[ang2pix] == 1
+                               (angular_filters.cpp:11-13); host array, NULL = off */
+    int64_t mask_nside;
+    uint64_t seed;          /* u of record i = SplitMix64 hash of (seed, index0 + i), uniform in [0, 1) */
+    uint64_t index0;
+};
+
+/* Convert and filter n host records; the kept points, (r, theta, phi) float64 in input
+ * order, go to points_out (host, room for n x 3) and their number to *n_out.  The
+ * reference's Filter swaps each rejected point with the last unread one (Filter.cpp:
+ * 25-35), so its survivors come out permuted; the SFB does not depend on the order
+ * beyond rounding. */
+catana_status_t catana_gpu_ingest(const void *records, int64_t n, const catana_ingest_t *spec, double *points_out,
+                                  int64_t *n_out, catana_gpu_stream_t stream);
 
 /* HEALPix (pixelized) SFB decomposition.  The catalog is given binned: pixel p
  * (RING scheme) holds the radii r_sorted[pix_offsets[p] .. pix_offsets[p+1]), in

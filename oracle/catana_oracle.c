@@ -742,3 +742,92 @@ void co_cartesian_to_spherical(const double *xyz, int64_t n, double *rtp)
         rtp[3 * i + 2] = ph;
     }
 }
+
+/* Ingest: record conversion (Point.cpp:5-10 for Cartesian records, as given for
+ * spherical ones, Point.cpp:23-28) and the point filters -- tophat r < R0
+ * (radial_filters.cpp:32-34), Gaussian exp(-(r/R0)^2) > u (:26-28), an interpolated
+ * generic window w(r) > u (:12-24 with FunctionInterpolator.cpp:6-30), a RING angular
+ * mask map[ang2pix] == 1 (angular_filters.cpp:11-13) -- with u of record i the
+ * SplitMix64 hash of (seed, index0 + i).  Kept points in input order.  Returns 0, or 2
+ * when a radius leaves the window's range / a theta leaves [0, pi] under a mask. */
+static double co_ingest_uniform(uint64_t seed, uint64_t index)
+{
+    uint64_t z = seed + (index + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53;
+}
+
+int co_ingest(const void *records, int64_t n, unsigned layout, double tophat_r0, double gauss_r0,
+              const double *window, int64_t window_n, double window_min, double window_max, const float *mask,
+              int64_t mask_nside, uint64_t seed, uint64_t index0, double *out, int64_t *n_out)
+{
+    int64_t k = 0;
+    int err = 0;
+    double dx_inv = 0.0;
+    if (window) dx_inv = 1.0 / ((window_max - window_min) / (double)(window_n - 1));
+    for (int64_t i = 0; i < n; ++i) {
+        double a, b, c, r, th, ph;
+        if (layout & 1u) {
+            const float *p = (const float *)records + 3 * i;
+            a = p[0];
+            b = p[1];
+            c = p[2];
+        } else {
+            const double *p = (const double *)records + 3 * i;
+            a = p[0];
+            b = p[1];
+            c = p[2];
+        }
+        if (layout & 2u) {
+            double v[3] = {a, b, c}, o[3];
+            co_cartesian_to_spherical(v, 1, o);
+            r = o[0];
+            th = o[1];
+            ph = o[2];
+        } else {
+            r = a;
+            th = b;
+            ph = c;
+        }
+        int keep = 1;
+        if (tophat_r0 > 0.0 && !(r < tophat_r0)) keep = 0;
+        if (keep && (gauss_r0 > 0.0 || window)) {
+            double u = co_ingest_uniform(seed, index0 + (uint64_t)i);
+            if (gauss_r0 > 0.0) {
+                double q = r / gauss_r0;
+                if (!(exp(-(q * q)) > u)) keep = 0;
+            }
+            if (keep && window) {
+                if (r < window_min || r >= window_max) {
+                    err = 2;
+                    keep = 0;
+                } else {
+                    double x = r - window_min, ia = x * dx_inv;
+                    unsigned ii = (unsigned)ia;
+                    if (ii > (unsigned)(window_n - 2)) ii = (unsigned)(window_n - 2); /* r just below the top */
+                    double w = window[ii] + (window[ii + 1] - window[ii]) * (ia - ii);
+                    if (!(w > u)) keep = 0;
+                }
+            }
+        }
+        if (keep && mask) {
+            int64_t pix = co_ang2pix_ring(mask_nside, th, ph);
+            if (pix < 0) {
+                err = 2;
+                keep = 0;
+            } else if (!(mask[pix] == 1.0f)) {
+                keep = 0;
+            }
+        }
+        if (keep) {
+            out[3 * k] = r;
+            out[3 * k + 1] = th;
+            out[3 * k + 2] = ph;
+            ++k;
+        }
+    }
+    *n_out = k;
+    return err;
+}

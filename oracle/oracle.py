@@ -71,6 +71,9 @@ def lib():
         L.co_sfb_healpix.argtypes = [_I64, _P, _P, _I, _I, _D, _I, _I, _P, _P, _P, _P]
         L.co_sfb_reverse.restype = _I
         L.co_sfb_reverse.argtypes = [_I64, _P, _P, _I, _I, _D, _I, _I, _P, _P, _P, _P]
+        L.co_ingest.restype = _I
+        L.co_ingest.argtypes = [_P, _I64, ctypes.c_uint, _D, _D, _P, _I64, _D, _D, _P, _I64, ctypes.c_uint64,
+                                ctypes.c_uint64, _P, _P]
         L.co_cartesian_to_spherical.restype = None
         L.co_cartesian_to_spherical.argtypes = [_P, _I64, _P]
         _lib = L
@@ -228,3 +231,24 @@ def sfb_healpix(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, store_
     if rc == 2:
         raise ValueError("argument (z) outside of defined range.")
     return k, c, _unpack_f(fre, fim, lmax, nmax) if store_flmn else []
+
+
+def ingest(records, cartesian=False, tophat_r0=0.0, gauss_r0=0.0, window=None, window_range=(0.0, 1.0), mask=None,
+           seed=0, index0=0):
+    """Record conversion and point filters (restatement of the device ingest; see
+    catana_oracle.c co_ingest).  records: (N, 3) float32 or float64."""
+    rec = np.ascontiguousarray(records)
+    f32 = rec.dtype == np.float32
+    rec = np.ascontiguousarray(rec, dtype=np.float32 if f32 else np.float64).reshape(-1, 3)
+    n = rec.shape[0]
+    out = np.zeros((max(n, 1), 3))
+    nout = np.zeros(1, dtype=np.int64)
+    win = None if window is None else np.ascontiguousarray(window, dtype=np.float64)
+    msk = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    mnside = 0 if msk is None else int(round(np.sqrt(msk.size / 12)))
+    rc = lib().co_ingest(_ptr(rec), n, (1 if f32 else 0) | (2 if cartesian else 0), float(tophat_r0), float(gauss_r0),
+                         _ptr(win), 0 if win is None else win.size, float(window_range[0]), float(window_range[1]),
+                         _ptr(msk), mnside, int(seed), int(index0), _ptr(out), _ptr(nout))
+    if rc == 2:
+        raise ValueError("ingest: radius outside the window's range or theta outside [0, pi]")
+    return out[:int(nout[0])].copy()

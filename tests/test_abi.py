@@ -139,3 +139,21 @@ def test_batched_argument_validation():
     assert _lib.lib.catana_gpu_sfb_raw_batched(None, -1, 0, 0.0, None) == _lib.ERR_ARG
     assert _lib.lib.catana_gpu_sfb_raw_batched(None, 0, 0, 0.0, None) == _lib.OK
     assert ctypes.sizeof(_lib.Catalog) == 72
+
+
+def test_ingest_spec_validation():
+    """The ingest entry point rejects bad specs before it touches a device."""
+    assert ctypes.sizeof(_lib.IngestSpec) == 88
+    sp = _lib.IngestSpec()
+    sp.layout = 8  # unknown bit
+    n_out = ctypes.c_int64(-1)
+    rec = np.zeros((2, 3))
+    out = np.zeros((2, 3))
+    assert _lib.lib.catana_gpu_ingest(_lib.ptr(rec), 2, ctypes.byref(sp), _lib.ptr(out), ctypes.byref(n_out),
+                                      None) == _lib.ERR_ARG
+    sp.layout, sp.mask_nside = 0, 3
+    sp.mask = rec.ctypes.data
+    assert _lib.lib.catana_gpu_ingest(_lib.ptr(rec), 2, ctypes.byref(sp), _lib.ptr(out), ctypes.byref(n_out),
+                                      None) == _lib.ERR_ARG
+    with pytest.raises(RuntimeError):
+        catana.ingest(rec, coordinate_type="polar")

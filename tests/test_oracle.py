@@ -176,3 +176,26 @@ def test_reverse_equals_fft_path_away_from_aliasing():
     # l = 0, 1: every ring has >= 4 pixels > 2 l, no alias
     for l in (0, 1):
         assert np.max(np.abs(f1[l] - f2[l])) <= 1e-12 * np.max(np.abs(f2[l]))
+
+
+def test_oracle_ingest_filters():
+    """Ingest restatement: conversion as Point(x, y, z); the tophat keeps exactly r < R0;
+    the Gaussian window keeps a fraction matching its expectation; the mask keeps
+    exactly the points whose RING pixel is 1; chunked calls (index0) reproduce one call."""
+    rng = np.random.default_rng(3)
+    xyz = rng.normal(size=(20000, 3)) * 300.0
+    rtp = O.cartesian_to_spherical(xyz)
+    assert np.array_equal(O.ingest(xyz, cartesian=True), rtp)
+    top = O.ingest(rtp, tophat_r0=400.0)
+    assert np.array_equal(top, rtp[rtp[:, 0] < 400.0])
+    g = O.ingest(rtp, gauss_r0=300.0, seed=11)
+    expect = np.exp(-(rtp[:, 0] / 300.0) ** 2).sum()
+    assert abs(g.shape[0] - expect) < 5 * np.sqrt(expect)
+    nside = 8
+    mask = (np.arange(12 * nside * nside) % 3 == 0).astype(np.float32)
+    pix = O.ang2pix_ring(nside, rtp[:, 1], rtp[:, 2])
+    assert np.array_equal(O.ingest(rtp, mask=mask), rtp[mask[pix] == 1.0])
+    both = O.ingest(rtp, gauss_r0=300.0, seed=11, mask=mask)
+    parts = np.concatenate([O.ingest(rtp[:7000], gauss_r0=300.0, seed=11, mask=mask),
+                            O.ingest(rtp[7000:], gauss_r0=300.0, seed=11, mask=mask, index0=7000)])
+    assert np.array_equal(both, parts)
