@@ -74,6 +74,7 @@ SIGNATURES = {
     "catana_gpu_pix2ang_ring": (ctypes.c_int, [_I64, _P, _I64, _P, _P, _P]),
     "catana_gpu_sbessel_zeros": (ctypes.c_int, [_U32, _I32, _P]),
     "catana_gpu_compute_kln": (ctypes.c_int, [_U16, _U16, _D, _P]),
+    "catana_gpu_sbessel_integrals": (ctypes.c_int, [_P, _I64, _D, _D, _U32, _D, _P, _P, _I64, _P, _P]),
     "catana_gpu_last_error": (ctypes.c_char_p, []),
     "catana_gpu_profile_enable": (None, [ctypes.c_int]),
     "catana_gpu_profile_report": (ctypes.c_int, [_P, _P, _P]),

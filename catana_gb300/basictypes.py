@@ -183,3 +183,35 @@ class PixelizedPointContainer(object):
 
     def __len__(self):
         return self.npix
+
+
+class FunctionInterpolator(object):
+    """Linear interpolation of a function on equally spaced nodes
+    (FunctionInterpolator.cpp:6-30; python/py_basictypes.cpp:173-215):
+    ``FunctionInterpolator(fct, interpolation_points, x_min, x_max)``; calling it
+    outside [x_min, x_max) raises ValueError.  The table also feeds the GPU integrals
+    of ``besseltools.double_sbessel_integrator``."""
+
+    def __init__(self, fct, interpolation_points, x_min, x_max):
+        n = int(interpolation_points)
+        if n < 2 or not (x_max > x_min):
+            raise ValueError("need interpolation_points >= 2 and x_min < x_max")
+        self.x_min, self.x_max, self.n = float(x_min), float(x_max), n
+        dx = (self.x_max - self.x_min) / (n - 1)
+        self._dx_inv = 1.0 / dx
+        xs = self.x_min + np.arange(n) * dx
+        try:
+            ys = np.asarray(fct(xs), dtype=np.float64)
+            if ys.shape != xs.shape:
+                raise ValueError
+        except Exception:
+            ys = np.array([float(fct(float(x))) for x in xs])
+        self.y_values = np.ascontiguousarray(ys)
+
+    def __call__(self, x):
+        x = float(x)
+        if x < self.x_min or x >= self.x_max:
+            raise ValueError("argument outside range for which this FunctionInterpolator is defined")
+        ia = (x - self.x_min) * self._dx_inv
+        i = int(ia)
+        return float(self.y_values[i] + (self.y_values[i + 1] - self.y_values[i]) * (ia - i))

@@ -272,6 +272,18 @@ catana_status_t catana_gpu_pix2ang_ring(int64_t nside, const int64_t *pix, int64
  * its Newton stopping rule.  Cached per process. */
 catana_status_t catana_gpu_sbessel_zeros(uint32_t l, int32_t count, double *out);
 
+/* Batched double spherical-Bessel integrals (the shot-noise integrals):
+ *   out[p] = int_0^r_max w(r) j_l(k1[p] r) j_l(k2[p] r) dr,  p < npairs,
+ * replacing besseltools::double_sbessel_integrator (sbessel_integrator.cpp:45-110,
+ * vectorised over k1, k2 in py_besseltools.cpp:45-84).  w is a FunctionInterpolator
+ * table: w_n values on equally spaced nodes of [w_min, w_max], linear in between
+ * (FunctionInterpolator.cpp:6-30); [0, r_max) must lie inside it (CATANA_ERR_DOMAIN
+ * otherwise, as the interpolator throws).  32-point Gauss-Legendre between the zeros of
+ * both Bessel factors.  Host arrays. */
+catana_status_t catana_gpu_sbessel_integrals(const double *w_table, int64_t w_n, double w_min, double w_max,
+                                             uint32_t l, double r_max, const double *k1, const double *k2,
+                                             int64_t npairs, double *out, catana_gpu_stream_t stream);
+
 /* k_ln = z_{l,n} / rmax for l < lmax, n < nmax, row-major (return_types.cpp:10-20). */
 catana_status_t catana_gpu_compute_kln(uint16_t lmax, uint16_t nmax, double rmax, double *k_ln);
 

@@ -831,3 +831,127 @@ int co_ingest(const void *records, int64_t n, unsigned layout, double tophat_r0,
     *n_out = k;
     return err;
 }
+
+/* Double spherical-Bessel integral int_0^rmax w(r) j_l(k1 r) j_l(k2 r) dr
+ * (sbessel_integrator.cpp:53-110): breakpoints at the zeros of both factors inside
+ * (0, rmax) (the reference's nested range generators, :113-133, visit the same merged
+ * set) and at the nodes of the w table (w linear on every piece), adaptive
+ * Gauss-Legendre on each piece (16 vs 32 nodes, bisection until they
+ * agree to 1e-14) instead of QAG, over the whole range; w is a FunctionInterpolator
+ * table (FunctionInterpolator.cpp:6-30).  Returns 0, or 2 when w is evaluated outside
+ * its range. */
+static void co_gl_nodes(int n, double *x, double *w)
+{
+    for (int i = 0; i < (n + 1) / 2; ++i) {
+        double z = cos(CO_PI * (i + 0.75) / (n + 0.5)), pp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; ++j) {
+                double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            double dz = p1 / pp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        x[i] = -z;
+        x[n - 1 - i] = z;
+        w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+    }
+}
+
+typedef struct {
+    const double *wt;
+    int64_t wn;
+    double wmin, wmax, dxinv, k1, k2;
+    int l, err;
+    double x16[16], w16[16], x32[32], w32[32];
+} co_dsb_ctx;
+
+static double co_dsb_f(co_dsb_ctx *c, double x)
+{
+    /* x == wmax only from rounding at the range's end (the rule's nodes are interior):
+     * the interpolator's last segment gives y[n-1] there */
+    if (x < c->wmin || x > c->wmax) {
+        c->err = 2;
+        return 0.0;
+    }
+    double ia = (x - c->wmin) * c->dxinv;
+    unsigned ii = (unsigned)ia;
+    if (ii > (unsigned)(c->wn - 2)) ii = (unsigned)(c->wn - 2);
+    double w = c->wt[ii] + (c->wt[ii + 1] - c->wt[ii]) * (ia - ii);
+    return w * co_sbessel_jl(c->l, c->k1 * x) * co_sbessel_jl(c->l, c->k2 * x);
+}
+
+static double co_dsb_piece(co_dsb_ctx *c, double a, double b, int depth)
+{
+    double h = 0.5 * (b - a), s16 = 0.0, s32 = 0.0, a32 = 0.0;
+    for (int i = 0; i < 16; ++i) s16 += c->w16[i] * co_dsb_f(c, a + h * (c->x16[i] + 1.0));
+    for (int i = 0; i < 32; ++i) {
+        double f = co_dsb_f(c, a + h * (c->x32[i] + 1.0));
+        s32 += c->w32[i] * f;
+        a32 += c->w32[i] * fabs(f);
+    }
+    s16 *= h;
+    s32 *= h;
+    a32 *= h;
+    /* agreement to 1e-13 of the piece's integral of |f| (pieces that cancel to ~0 are
+     * judged on that scale, not on their own tiny sum) */
+    if (depth >= 12 || fabs(s32 - s16) <= 1e-13 * a32 + 1e-300) return s32;
+    double m = 0.5 * (a + b);
+    return co_dsb_piece(c, a, m, depth + 1) + co_dsb_piece(c, m, b, depth + 1);
+}
+
+int co_dsb_integral(const double *w_table, int64_t w_n, double w_min, double w_max, int l, double rmax, double k1,
+                    double k2, double *out)
+{
+    co_dsb_ctx c;
+    c.wt = w_table;
+    c.wn = w_n;
+    c.wmin = w_min;
+    c.wmax = w_max;
+    c.dxinv = 1.0 / ((w_max - w_min) / (double)(w_n - 1));
+    c.l = l;
+    c.err = 0;
+    if (k1 > k2) {
+        double t = k1;
+        k1 = k2;
+        k2 = t;
+    }
+    c.k1 = k1;
+    c.k2 = k2;
+    co_gl_nodes(16, c.x16, c.w16);
+    co_gl_nodes(32, c.x32, c.w32);
+    int nz = 2;
+    double *z = NULL;
+    for (;;) {
+        free(z);
+        z = (double *)malloc(sizeof(double) * nz);
+        co_sbessel_zeros((unsigned)l, nz, z);
+        if (z[nz - 1] > k2 * rmax) break;
+        nz *= 2;
+    }
+    double lo = 0.0, acc = 0.0, wdx = (w_max - w_min) / (double)(w_n - 1);
+    int i1 = 0, i2 = 0;
+    int64_t it = (int64_t)floor((0.0 - w_min) / wdx) + 1;
+    if (it < 1) it = 1;
+    if (w_min > 0.0 || rmax > w_max) c.err = 2;
+    while (lo < rmax && !c.err) {
+        /* breakpoints: table nodes (w linear between them) and the zeros of both factors */
+        double zt = (it < w_n) ? w_min + (double)it * wdx : INFINITY;
+        double z1 = (k1 > 0.0 && i1 < nz) ? z[i1] / k1 : INFINITY;
+        double z2 = (k2 > 0.0 && i2 < nz) ? z[i2] / k2 : INFINITY;
+        double hi = fmin(fmin(fmin(z1, z2), zt), rmax);
+        if (hi > lo) acc += co_dsb_piece(&c, lo, hi, 0);
+        if (zt <= hi) ++it;
+        if (z1 <= hi) ++i1;
+        if (z2 <= hi) ++i2;
+        if (hi >= rmax || (!(zt <= hi) && !(z1 <= hi) && !(z2 <= hi))) break;
+        lo = hi;
+    }
+    free(z);
+    *out = acc;
+    return c.err;
+}

@@ -74,6 +74,8 @@ def lib():
         L.co_ingest.restype = _I
         L.co_ingest.argtypes = [_P, _I64, ctypes.c_uint, _D, _D, _P, _I64, _D, _D, _P, _I64, ctypes.c_uint64,
                                 ctypes.c_uint64, _P, _P]
+        L.co_dsb_integral.restype = _I
+        L.co_dsb_integral.argtypes = [_P, _I64, _D, _D, _I, _D, _D, _D, _P]
         L.co_cartesian_to_spherical.restype = None
         L.co_cartesian_to_spherical.argtypes = [_P, _I64, _P]
         _lib = L
@@ -252,3 +254,15 @@ def ingest(records, cartesian=False, tophat_r0=0.0, gauss_r0=0.0, window=None, w
     if rc == 2:
         raise ValueError("ingest: radius outside the window's range or theta outside [0, pi]")
     return out[:int(nout[0])].copy()
+
+
+def dsb_integral(w_table, w_range, l, rmax, k1, k2):
+    """int_0^rmax w(r) j_l(k1 r) j_l(k2 r) dr with w a FunctionInterpolator table on
+    w_range (restatement of sbessel_integrator.cpp:53-110; see co_dsb_integral)."""
+    wt = np.ascontiguousarray(w_table, dtype=np.float64)
+    out = np.zeros(1)
+    rc = lib().co_dsb_integral(_ptr(wt), wt.size, float(w_range[0]), float(w_range[1]), int(l), float(rmax),
+                               float(k1), float(k2), _ptr(out))
+    if rc == 2:
+        raise ValueError("argument outside range for which this FunctionInterpolator is defined")
+    return float(out[0])

@@ -157,3 +157,23 @@ def test_ingest_spec_validation():
                                       None) == _lib.ERR_ARG
     with pytest.raises(RuntimeError):
         catana.ingest(rec, coordinate_type="polar")
+
+
+def test_function_interpolator_and_integral_validation():
+    """py_basictypes FunctionInterpolator behaviour (besseltools_test.py:39-53) and the
+    integrals entry's argument checks (no device needed)."""
+    w = lambda r: np.exp(-(r / 40) ** 2) * r ** 2
+    fi = catana.FunctionInterpolator(w, 100000, 0, 100)
+    assert fi(0) == w(0)
+    assert fi(99.9) == pytest.approx(w(99.9))
+    for bad in (100, -1, 120):
+        with pytest.raises(ValueError):
+            fi(bad)
+    k = np.ones(2)
+    out = np.zeros(2)
+    tab = np.ones(2)
+    assert _lib.lib.catana_gpu_sbessel_integrals(_lib.ptr(tab), 1, 0.0, 1.0, 0, 1.0, _lib.ptr(k), _lib.ptr(k), 2,
+                                                 _lib.ptr(out), None) == _lib.ERR_ARG
+    kneg = -np.ones(2)
+    assert _lib.lib.catana_gpu_sbessel_integrals(_lib.ptr(tab), 2, 0.0, 1.0, 0, 1.0, _lib.ptr(kneg), _lib.ptr(k), 2,
+                                                 _lib.ptr(out), None) == _lib.ERR_ARG

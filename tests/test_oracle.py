@@ -199,3 +199,15 @@ def test_oracle_ingest_filters():
     parts = np.concatenate([O.ingest(rtp[:7000], gauss_r0=300.0, seed=11, mask=mask),
                             O.ingest(rtp[7000:], gauss_r0=300.0, seed=11, mask=mask, index0=7000)])
     assert np.array_equal(both, parts)
+
+
+def test_oracle_dsb_integral_known_values():
+    """besseltools_test.py:26-37 and sbessel_integrator.cpp:8-14: known integrals with
+    w = 1, and symmetry in k1 <-> k2."""
+    one = np.ones(3)
+    assert O.dsb_integral(one, (0.0, 100.0 + 1e-9), 0, 100, 1, 1) == pytest.approx(1.56582, abs=1e-5)
+    assert O.dsb_integral(one, (0.0, 100.0 + 1e-9), 0, 100, 1, 2) == pytest.approx(0.785393, abs=1e-5)
+    assert O.dsb_integral(one, (0.0, 100.0 + 1e-9), 4, 100, 1, 4.2) == pytest.approx(0.000133933, abs=1e-9)
+    x = np.linspace(0.0, 100.0, 100000)
+    w = np.exp(-(x / 40) ** 2) * x ** 2
+    assert O.dsb_integral(w, (0, 100), 6, 100, 2.3, 4.5) == O.dsb_integral(w, (0, 100), 6, 100, 4.5, 2.3)
