@@ -8,12 +8,12 @@ errors.  The compute runs in libcatana_gpu.so (hand-written CUDA for sm_103a beh
 the C ABI in include/catana_gpu.h); there is no CPU fallback.
 """
 from . import _lib  # noqa: F401  (raises ImportError when the library is missing)
-from . import besseltools
+from . import besseltools, io
 from .basictypes import FunctionInterpolator, PixelizedPointContainer, Point, PointContainer
 from .decomposition import (KClkk, SFBAccumulator, compute_kln, ingest, sfb_decomposition,
                             sfb_decomposition_batched, sfb_decomposition_healpix, sfb_reverse)
 
 __all__ = ["Point", "PointContainer", "FunctionInterpolator", "PixelizedPointContainer", "KClkk", "sfb_decomposition",
            "sfb_decomposition_healpix", "sfb_decomposition_batched", "SFBAccumulator", "sfb_reverse", "ingest", "compute_kln",
-           "besseltools"]
+           "besseltools", "io"]
 __version__ = "0.1.0"

@@ -65,6 +65,7 @@ SIGNATURES = {
     "catana_gpu_accum_add": (ctypes.c_int, [_P, _P, _P, _I64]),
     "catana_gpu_accum_finish": (ctypes.c_int, [_P, _P, _P, _P]),
     "catana_gpu_accum_add_records": (ctypes.c_int, [_P, _P, _I64, _P]),
+    "catana_gpu_accum_add_file": (ctypes.c_int, [_P, ctypes.c_char_p, _I64, _I64, _I64, _P, _P]),
     "catana_gpu_ingest": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P]),
     "catana_gpu_accum_destroy": (ctypes.c_int, [_P]),
     "catana_gpu_sfb_healpix": (ctypes.c_int, [_I64, _P, _P, _U16, _U16, _D, _U32, _P, _P, _P, _P]),

@@ -14,8 +14,10 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -322,6 +324,75 @@ catana_status_t catana_gpu_accum_add_records(catana_gpu_accum_t acc, const void 
         return CATANA_ERR_ARG;
     }
     return accum_add_records(reinterpret_cast<Accum *>(acc), records, n, *spec);
+}
+
+catana_status_t catana_gpu_accum_add_file(catana_gpu_accum_t acc, const char *path, int64_t first_record,
+                                          int64_t max_records, int64_t chunk_records, const catana_ingest_t *spec,
+                                          int64_t *records_read) {
+    // RawBinarySource (RawBinarySource.cpp:6-61): a file of consecutive fixed-size records
+    // read in chunks; here a reader thread fills one of two pinned host buffers while the
+    // previous chunk is copied, filtered and decomposed.
+    if (records_read) *records_read = 0;
+    if (!acc || !path || !spec || first_record < 0 || chunk_records <= 0) {
+        set_error("add_file: null argument, negative first_record or non-positive chunk");
+        return CATANA_ERR_ARG;
+    }
+    const size_t rsz = (size_t)3 * ((spec->layout & CATANA_REC_FLOAT32) ? 4 : 8);
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) {
+        set_error(std::string("add_file: cannot open ") + path);
+        return CATANA_ERR_ARG;
+    }
+    std::fseek(fp, 0, SEEK_END);
+    const long long bytes = std::ftell(fp);
+    int64_t ntot = bytes > 0 ? (int64_t)(bytes / (long long)rsz) : 0;  // trailing partial record ignored
+    int64_t n = std::max<int64_t>(0, ntot - first_record);
+    if (max_records >= 0) n = std::min(n, max_records);
+    if (n == 0) {
+        std::fclose(fp);
+        return CATANA_OK;
+    }
+    std::fseek(fp, (long)((long long)first_record * (long long)rsz), SEEK_SET);
+    const int64_t chunk = std::min(chunk_records, n);
+    void *buf[2] = {nullptr, nullptr};
+    for (int k = 0; k < 2; ++k)
+        if (cudaHostAlloc(&buf[k], (size_t)chunk * rsz, cudaHostAllocDefault) != cudaSuccess) {
+            if (buf[0]) cudaFreeHost(buf[0]);
+            std::fclose(fp);
+            set_error("add_file: cudaHostAlloc failed");
+            return CATANA_ERR_NOMEM;
+        }
+    auto read_into = [&](int k, int64_t cnt) -> int64_t {
+        return (int64_t)std::fread(buf[k], rsz, (size_t)cnt, fp);
+    };
+    catana_status_t s = CATANA_OK;
+    int64_t done = 0, got = read_into(0, std::min(chunk, n));
+    int cur = 0;
+    while (got > 0 && s == CATANA_OK) {
+        const int64_t todo = std::min(chunk, n - done - got);
+        int64_t got_next = 0;
+        std::thread reader;
+        if (todo > 0) reader = std::thread([&, cur, todo]() { got_next = read_into(cur ^ 1, todo); });
+        catana_ingest_t sp = *spec;
+        sp.index0 = spec->index0 + (uint64_t)(first_record + done);
+        s = accum_add_records(reinterpret_cast<Accum *>(acc), buf[cur], got, sp);
+        if (reader.joinable()) reader.join();
+        done += got;
+        // the chunk in buf[cur] is read by the copy of the next add (pinned, asynchronous):
+        // wait for the device to be done with it before it is refilled
+        Accum *A = reinterpret_cast<Accum *>(acc);
+        cudaStreamSynchronize(A->copy_st);
+        got = got_next;
+        cur ^= 1;
+    }
+    Accum *A = reinterpret_cast<Accum *>(acc);
+    cudaStreamSynchronize(A->copy_st);
+    cudaStreamSynchronize(A->comp_st);
+    cudaFreeHost(buf[0]);
+    cudaFreeHost(buf[1]);
+    std::fclose(fp);
+    if (records_read) *records_read = done;
+    return s;
 }
 
 catana_status_t catana_gpu_accum_finish(catana_gpu_accum_t acc, double *k_ln, double *c_ln, double *f_lmn) {

@@ -336,6 +336,24 @@ class SFBAccumulator(object):
         self._records_seen = int(index0) + rec.shape[0]
         self._keep = (self._keep + [tuple(keep)])[-2:]
 
+    def add_file(self, filename, coordinate_type="spherical", dtype=np.float32, first_record=0, max_records=-1,
+                 chunk=8_000_000, tophat_r0=None, gauss_r0=None, window=None, window_range=(0.0, 1.0), mask=None,
+                 seed=0):
+        """Stream a raw binary record file (the RawBinarySource format: consecutive records
+        of 3 float32 or float64, Cartesian or spherical) through the GPU ingest into this
+        accumulation, `chunk` records at a time; file reads overlap the decomposition.
+        Returns the number of records read."""
+        dt = np.dtype(dtype)
+        if dt not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise ValueError("dtype must be float32 or float64")
+        proto = np.zeros((1, 3), dtype=dt)
+        _, sp, keep = _ingest_spec(proto, coordinate_type, tophat_r0, gauss_r0, window, window_range, mask, seed, 0)
+        n = ctypes.c_int64(0)
+        _lib.check(_lib.lib.catana_gpu_accum_add_file(self._h, str(filename).encode(), int(first_record),
+                                                      int(max_records), int(chunk), ctypes.byref(sp),
+                                                      ctypes.byref(n)), "accum_add_file")
+        return n.value
+
     def finish(self, store_flmn=False):
         k = np.zeros((self.lmax, self.nmax))
         c = np.zeros((self.lmax, self.nmax))

@@ -191,6 +191,15 @@ catana_status_t catana_gpu_accum_add(catana_gpu_accum_t acc, const double *point
  * decomposed; no weights */
 catana_status_t catana_gpu_accum_add_records(catana_gpu_accum_t acc, const void *records, int64_t n,
                                              const catana_ingest_t *spec);
+/* records [first_record, first_record + max_records) of a raw binary file (the
+ * RawBinarySource format, RawBinarySource.cpp:6-61: consecutive records of 3 floats or
+ * 3 doubles, Cartesian or spherical per spec->layout; max_records < 0 = to the end),
+ * read chunk_records at a time into pinned buffers by a reader thread while the
+ * previous chunk is filtered and decomposed as in add_records (index0 of the random
+ * windows advances with the record number).  *records_read receives the count. */
+catana_status_t catana_gpu_accum_add_file(catana_gpu_accum_t acc, const char *path, int64_t first_record,
+                                          int64_t max_records, int64_t chunk_records, const catana_ingest_t *spec,
+                                          int64_t *records_read);
 catana_status_t catana_gpu_accum_finish(catana_gpu_accum_t acc, double *k_ln, double *c_ln, double *f_lmn);
 catana_status_t catana_gpu_accum_destroy(catana_gpu_accum_t acc);
 

@@ -177,3 +177,19 @@ def test_function_interpolator_and_integral_validation():
     kneg = -np.ones(2)
     assert _lib.lib.catana_gpu_sbessel_integrals(_lib.ptr(tab), 2, 0.0, 1.0, 0, 1.0, _lib.ptr(kneg), _lib.ptr(k), 2,
                                                  _lib.ptr(out), None) == _lib.ERR_ARG
+
+
+def test_raw_binary_roundtrip(tmp_path):
+    """RawBinarySink / RawBinarySource record format: 12- or 24-byte records, no header;
+    Cartesian records read back through Point(x, y, z)."""
+    pts = O.cartesian_to_spherical(np.random.default_rng(5).normal(size=(500, 3)) * 100)
+    f32 = tmp_path / "pts_f32.bin"
+    catana.io.write_raw_binary(str(f32), pts, "spherical", np.float32)
+    assert f32.stat().st_size == 500 * 12
+    back = np.asarray(catana.io.read_raw_binary(str(f32), "spherical", np.float32))
+    assert np.array_equal(back, pts.astype(np.float32).astype(np.float64))
+    f64 = tmp_path / "pts_c64.bin"
+    catana.io.write_raw_binary(str(f64), pts, "cartesian", np.float64)
+    assert f64.stat().st_size == 500 * 24
+    back = np.asarray(catana.io.read_raw_binary(str(f64), "cartesian", np.float64))
+    assert np.allclose(back, pts, rtol=1e-12, atol=1e-12)
