@@ -409,6 +409,69 @@ def streamed_workload(torch, _lib, catana, chunks=2, chunk=8_000_000, L=512, M=2
     return out
 
 
+def next_rows_workload(torch, _lib, catana):
+    """The survey's "next" rows, one timing each:
+    * _sfb_reverse on the HEALPix workload (nside 256, 1M points, lmax 128, nmax 64);
+    * device ingest of 8M float32 Cartesian records (tophat + Gaussian window + angular
+      mask): records/s and the kernels' HBM bytes per record;
+    * shot-noise integrals: all (n1, n2) pairs for l < 32, nmax 32 (32k integrals) with
+      a 10001-node window table, against the oracle's CPU quadrature on 64 of them."""
+    res = {}
+    rng = np.random.default_rng(1)
+    pts, _ = catalog(1_000_000, 1000.0, 1)
+    ppc = catana.PixelizedPointContainer(256, catana.PointContainer(pts))
+    catana.sfb_reverse(ppc, 128, 64, 1000.0, False, False)
+    t0 = time.perf_counter()
+    catana.sfb_reverse(ppc, 128, 64, 1000.0, False, False)
+    res["sfb_reverse_nside256_1M_l128_n64_s"] = time.perf_counter() - t0
+    # ingest
+    n = 8_000_000
+    xyz = (rng.normal(size=(n, 3)) * 500.0).astype(np.float32)
+    mask = (rng.random(12 * 64 * 64) < 0.7).astype(np.float32)
+    kw = dict(coordinate_type="cartesian", tophat_r0=1500.0, gauss_r0=1000.0, mask=mask, seed=3)
+    catana.ingest(xyz[:100000], **kw)
+    t0 = time.perf_counter()
+    kept = catana.ingest(xyz, **kw)
+    dt = time.perf_counter() - t0
+    res["ingest_8M_float32_cartesian"] = {"records_per_s": n / dt, "seconds": dt, "kept": len(kept),
+                                          "note": "host API incl. 96 MB H2D and the kept points D2H",
+                                          "device_bytes_per_record": 12 + 24 + 1 + 24 + 1}
+    # integrals
+    rmax = 1000.0
+    fi = catana.FunctionInterpolator(lambda r: np.exp(-(r / 400.0) ** 2) * r ** 2, 10001, 0.0, rmax)
+    L, M = 32, 32
+    kk = catana.compute_kln(L, M, rmax)
+    total = 0
+    catana.besseltools.double_sbessel_integrator(fi, 1, rmax, kk[1][:2], kk[1][:2])
+    t0 = time.perf_counter()
+    for l in range(L):
+        k1, k2 = np.meshgrid(kk[l], kk[l])
+        catana.besseltools.double_sbessel_integrator(fi, l, rmax, k1, k2)
+        total += k1.size
+    dt = time.perf_counter() - t0
+    res["shot_noise_integrals_l32_n32"] = {"integrals": total, "seconds": dt, "integrals_per_s": total / dt,
+                                           "note": "one warp per pair, 32/8-point Gauss-Legendre between the zeros "
+                                                   "and the window's nodes; host API incl. copies"}
+    return res
+
+
+def cpu_integrals_baseline():
+    """The oracle's quadrature of the same integrals (adaptive Gauss-Legendre, one core)
+    on 64 of them: the CPU side of the shot-noise-integral leg."""
+    from oracle import oracle as O
+    rmax = 1000.0
+    x = np.linspace(0.0, rmax, 10001)
+    w = np.exp(-(x / 400.0) ** 2) * x ** 2
+    import catana_gb300 as catana
+    kk = catana.compute_kln(32, 32, rmax)
+    t0 = time.perf_counter()
+    for i in range(8):
+        for j in range(8):
+            O.dsb_integral(w, (0.0, rmax), 16, rmax, kk[16][i], kk[16][j])
+    return {"value": 64 / (time.perf_counter() - t0), "unit": "integrals/s", "cores": 1, "kind": "port",
+            "sample": "64 (n1, n2) pairs at l = 16 of the same window and k_ln"}
+
+
 def workload_config(a):
     return {"workload": "raw SFB %s form: %d points uniform in a ball rmax=%g, weights U[0.5,1.5], lmax=%d, "
                         "nmax=%d, seed %d" % (a.form, a.points, a.rmax, a.lmax, a.nmax, a.seed),
@@ -606,12 +669,15 @@ def main():
         if a.side:
             out["side"] = side_workloads(torch, _lib, catana, sp)
             out["side"]["batched_64_catalogs_kmax0.2_split"] = batched_workload(torch, _lib, catana, sp)
+            out["side"]["next_rows"] = next_rows_workload(torch, _lib, catana)
             if a.stream_chunks > 0:
                 out["side"]["streamed_survey_l512_n256_split"] = streamed_workload(torch, _lib, catana,
                                                                                   chunks=a.stream_chunks)
         # ---- CPU baseline: the oracle's OpenMP restatement on a bounded sample ----
         cs = min(a.cpu_sample, a.points)
         v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
+        if a.side:
+            out["side"]["next_rows"]["shot_noise_integrals_l32_n32"]["cpu_baseline"] = cpu_integrals_baseline()
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": "%d points (of %d), same lmax/nmax/rmax/weights, interpolated j_l as the "
                                          "reference uses for N > 1000; %.1f s" % (cs, a.points, dt)}
