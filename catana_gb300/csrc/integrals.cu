@@ -11,9 +11,10 @@
 // (0, rmax) -- plus the nodes of the w table, so that w is linear on every piece (w is a
 // FunctionInterpolator table, FunctionInterpolator.cpp:6-30: linear on equally spaced
 // nodes, domain error outside [x_min, x_max); its kinks would otherwise cost GL its
-// accuracy).  Each piece takes a 32-point Gauss-Legendre rule (one node per lane), or an
-// 8-point one when it is shorter than 1/(4 k2) -- fine tables -- and the whole range is
-// summed.
+// accuracy).  Between consecutive zeros the warp spreads the table segments over its
+// lanes with a Gauss-Legendre rule chosen by the segment length L: 2 points for
+// k2 L <= 0.02, 4 for <= 0.1, 8 for <= 0.25, else 32 (error below 1e-10 of the
+// segment's integral in every case); the whole range is summed.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,7 +28,17 @@ namespace catana_gpu {
 
 namespace {
 
-constexpr int GL_N = 32;
+
+// GL rules packed in one array: 2 points at [0, 2), 4 at [2, 6), 8 at [6, 14), 32 at [14, 46)
+constexpr int GL_OFF2 = 0, GL_OFF4 = 2, GL_OFF8 = 6, GL_OFF32 = 14, GL_TOT = 46;
+
+__device__ __forceinline__ double dsb_w(const double *__restrict__ wt, int64_t wn, double wmin, double wdxinv,
+                                        double x) {
+    const double ia = (x - wmin) * wdxinv;  // FunctionInterpolator form; x may round onto wmax at the end
+    unsigned ii = (unsigned)ia;
+    if (ii > (unsigned)(wn - 2)) ii = (unsigned)(wn - 2);
+    return wt[ii] + (wt[ii + 1] - wt[ii]) * (ia - ii);
+}
 
 __global__ void k_dsb_integrals(const double *__restrict__ zeros, int nz, const double *__restrict__ glx,
                                 const double *__restrict__ glw, const double *__restrict__ wt, int64_t wn,
@@ -43,47 +54,50 @@ __global__ void k_dsb_integrals(const double *__restrict__ zeros, int nz, const 
         a = b;
         b = t;
     }
-    // nodes: glx/glw[0..31] 32-point rule, [32..39] 8-point rule
-    const double x32 = glx[lane], w32 = glw[lane];
-    const double x8 = glx[32 + (lane & 7)], w8 = glw[32 + (lane & 7)];
-    const double short_len = b > 0.0 ? 0.25 / b : INFINITY;  // a piece this short: 8 points suffice
     double acc = 0.0;
     int i1 = 0, i2 = 0;
-    int64_t it = (int64_t)floor((0.0 - wmin) * wdxinv) + 1;  // next table node above 0
-    if (it < 1) it = 1;
     double lo = 0.0;
-    int bad = (wmin > 0.0 || rmax > wmax) ? 1 : 0;
+    const int bad = (wmin > 0.0 || rmax > wmax) ? 1 : 0;
     while (lo < rmax && !bad) {
-        const double zt = (it < wn) ? wmin + (double)it * wdx : INFINITY;
+        // the next zero of either factor: the Bessel product keeps its sign up to there
         const double z1 = (a > 0.0 && i1 < nz) ? zeros[i1] / a : INFINITY;
         const double z2 = (b > 0.0 && i2 < nz) ? zeros[i2] / b : INFINITY;
-        const double hi = fmin(fmin(fmin(z1, z2), zt), rmax);
+        const double hi = fmin(fmin(z1, z2), rmax);
         if (hi > lo) {
-            const double half = 0.5 * (hi - lo);
-            const bool use8 = (hi - lo) < short_len;
-            double x, wg;
-            if (use8) {
-                x = lo + half * (x8 + 1.0);
-                wg = lane < 8 ? w8 : 0.0;
-            } else {
-                x = lo + half * (x32 + 1.0);
-                wg = w32;
+            // table nodes strictly inside (lo, hi) split it into segments on which w is linear
+            int64_t ilo = (int64_t)floor((lo - wmin) * wdxinv) + 1;
+            while (ilo > 0 && wmin + (double)(ilo - 1) * wdx > lo) --ilo;
+            while (wmin + (double)ilo * wdx <= lo) ++ilo;
+            int64_t ihi = ilo - 1;
+            {
+                int64_t c = (int64_t)ceil((hi - wmin) * wdxinv) - 1;
+                while (c >= ilo && wmin + (double)c * wdx >= hi) --c;
+                while (wmin + (double)(c + 1) * wdx < hi && c + 1 < wn) ++c;
+                ihi = c;
             }
-            if (wg != 0.0) {
-                // w is linear on the piece (no table node inside): FunctionInterpolator form;
-                // a node can round onto wmax at the end of the range, where the last
-                // segment gives y[n-1]
-                const double ia = (x - wmin) * wdxinv;
-                unsigned ii = (unsigned)ia;
-                if (ii > (unsigned)(wn - 2)) ii = (unsigned)(wn - 2);
-                const double w = wt[ii] + (wt[ii + 1] - wt[ii]) * (ia - ii);
-                acc += wg * half * w * sbessel_jl(l, a * x) * sbessel_jl(l, b * x);
+            const int64_t nseg = (ihi >= ilo) ? ihi - ilo + 2 : 1;
+            const double seglen = (nseg > 1) ? wdx : (hi - lo);
+            // rule per segment length (k2 len: <= 0.02 -> 2 points, 0.1 -> 4, 0.25 -> 8, else 32)
+            const double kl = b * seglen;
+            const int npg = kl <= 0.02 ? 2 : (kl <= 0.1 ? 4 : (kl <= 0.25 ? 8 : 32));
+            const int goff = npg == 2 ? GL_OFF2 : (npg == 4 ? GL_OFF4 : (npg == 8 ? GL_OFF8 : GL_OFF32));
+            const int per = 32 / npg;  // segments per warp pass
+            const int j = lane % npg;
+            const double xg = glx[goff + j], wg = glw[goff + j];
+            for (int64_t s0 = 0; s0 < nseg; s0 += per) {
+                const int64_t sgi = s0 + lane / npg;
+                if (sgi < nseg) {
+                    const double sa = (sgi == 0) ? lo : wmin + (double)(ilo + sgi - 1) * wdx;
+                    const double sb = (sgi == nseg - 1) ? hi : wmin + (double)(ilo + sgi) * wdx;
+                    const double half = 0.5 * (sb - sa);
+                    const double x = sa + half * (xg + 1.0);
+                    acc += wg * half * dsb_w(wt, wn, wmin, wdxinv, x) * sbessel_jl(l, a * x) * sbessel_jl(l, b * x);
+                }
             }
         }
-        if (zt <= hi) ++it;
         if (z1 <= hi) ++i1;
         if (z2 <= hi) ++i2;
-        if (hi >= rmax || (!(zt <= hi) && !(z1 <= hi) && !(z2 <= hi))) break;
+        if (hi >= rmax || (!(z1 <= hi) && !(z2 <= hi))) break;
         lo = hi;
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -153,11 +167,13 @@ catana_status_t catana_gpu_sbessel_integrals(const double *w_table, int64_t w_n,
     if (!ctx) return (catana_status_t)cs;
     std::lock_guard<std::mutex> g(ctx->mu);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    std::vector<double> glx(GL_N + 8), glw(GL_N + 8);
-    gauss_legendre(GL_N, glx.data(), glw.data());
-    gauss_legendre(8, glx.data() + GL_N, glw.data() + GL_N);
+    std::vector<double> glx(GL_TOT), glw(GL_TOT);
+    gauss_legendre(2, glx.data() + GL_OFF2, glw.data() + GL_OFF2);
+    gauss_legendre(4, glx.data() + GL_OFF4, glw.data() + GL_OFF4);
+    gauss_legendre(8, glx.data() + GL_OFF8, glw.data() + GL_OFF8);
+    gauss_legendre(32, glx.data() + GL_OFF32, glw.data() + GL_OFF32);
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t zb = al((size_t)nz * 8), gb = al(2 * (GL_N + 8) * 8), wb = al((size_t)w_n * 8), kb = al((size_t)npairs * 8);
+    const size_t zb = al((size_t)nz * 8), gb = al(2 * GL_TOT * 8), wb = al((size_t)w_n * 8), kb = al((size_t)npairs * 8);
     CG_CUDA_TRY(ctx->io_points.ensure(zb + gb + wb + 3 * kb + 256));
     char *d = ctx->io_points.as<char>();
     double *zd = reinterpret_cast<double *>(d), *gd = reinterpret_cast<double *>(d + zb),
@@ -165,8 +181,8 @@ catana_status_t catana_gpu_sbessel_integrals(const double *w_table, int64_t w_n,
            *k2d = reinterpret_cast<double *>(d + zb + gb + wb + kb),
            *od = reinterpret_cast<double *>(d + zb + gb + wb + 2 * kb);
     CG_CUDA_TRY(cudaMemcpyAsync(zd, z, (size_t)nz * 8, cudaMemcpyHostToDevice, st));
-    CG_CUDA_TRY(cudaMemcpyAsync(gd, glx.data(), (GL_N + 8) * 8, cudaMemcpyHostToDevice, st));
-    CG_CUDA_TRY(cudaMemcpyAsync(gd + GL_N + 8, glw.data(), (GL_N + 8) * 8, cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(gd, glx.data(), GL_TOT * 8, cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(gd + GL_TOT, glw.data(), GL_TOT * 8, cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(wd, w_table, (size_t)w_n * 8, cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(k1d, k1, (size_t)npairs * 8, cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(k2d, k2, (size_t)npairs * 8, cudaMemcpyHostToDevice, st));
@@ -175,7 +191,7 @@ catana_status_t catana_gpu_sbessel_integrals(const double *w_table, int64_t w_n,
     CG_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
     const double wdx = (w_max - w_min) / (double)(w_n - 1), wdxinv = 1.0 / wdx;
     const int64_t threads = npairs * 32;
-    k_dsb_integrals<<<ceil_div(threads, 256), 256, 0, st>>>(zd, nz, gd, gd + GL_N + 8, wd, w_n, w_min, w_max, wdx,
+    k_dsb_integrals<<<ceil_div(threads, 256), 256, 0, st>>>(zd, nz, gd, gd + GL_TOT, wd, w_n, w_min, w_max, wdx,
                                                             wdxinv, (int)l, r_max, k1d, k2d, npairs, od, err);
     count_launch();
     CG_CUDA_TRY(cudaGetLastError());
