@@ -184,6 +184,11 @@ __device__ __forceinline__ void store_split4p(uint8_t *hi_base, uint8_t *lo_base
     *reinterpret_cast<uint2 *>(lo_base + off) = make_uint2(o[0], o[1]);
 }
 
+// 2-bit row exponent of point q from an exponent word (bit q of each half)
+__device__ __forceinline__ unsigned ebits(unsigned long long w, int q) {
+    return (unsigned)((w >> q) & 1ull) | ((unsigned)((w >> (32 + q)) & 1ull) << 1);
+}
+
 // Y column order inside each 8-column group of complex m0..m0+3:
 //   Re m0, Re m0+1, Im m0, Im m0+1, Re m0+2, Re m0+3, Im m0+2, Im m0+3
 // (value pairs of consecutive m stay adjacent for the packed arithmetic).
@@ -204,7 +209,10 @@ __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c
 // P * 2^100 * 2^(128 e); e grows by one when a sectoral value drops below 2^-40 and
 // shrinks by one when a value grows past 2^40 along l, so seeds down to ~2^-520 stay
 // exact.  Values with e > 0 are below 2^-188 and enter Y as zero.
-template <bool EXT>
+// FULLJ: every item of the launch has 128 radial orders in its half (no kmax cut):
+// each warp evaluates 8 J rows; otherwise the items' live row pairs are spread over
+// the warps and the rest of J stays zero.
+template <bool EXT, bool FULLJ>
 __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -256,6 +264,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         tc05::mbar_init(&sbar[0], 1);
         tc05::mbar_init(&sbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // J rows of radial orders past this half's count (a kmax cut, or nmax < 128) are zero
+    // for the whole item: zero both operand buffers' J now; warps whose 8 rows are all
+    // past the count then skip J entirely
+    if (!FULLJ && nmax < NHALF) {
+        for (int t = tid; t < (int)(2 * SM_J / 16); t += NTHR) {
+            *reinterpret_cast<uint4 *>(sm + t * 16) = make_uint4(0u, 0u, 0u, 0u);            // buffer 0
+            *reinterpret_cast<uint4 *>(sm + SM_BUF + t * 16) = make_uint4(0u, 0u, 0u, 0u);  // buffer 1
+        }
     }
     if (warp == 0) tc05::tmem_alloc(&tmem_base_sh, tcols);
     tc05::fence_before();
@@ -425,8 +442,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
                                                                 2 * SM_STROW + q * 48);
         const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
-        // ---- J tile: n = 8 g .. 8 g + 7 (zero past this half's count) ----
-        {
+        // ---- J tile: n = 8 g .. 8 g + 7 ----
+        if constexpr (FULLJ) {
             const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
             const float2 w2 = make_float2(pt.w, pt.w);
             const int n0 = 8 * g;
@@ -464,6 +481,48 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
             }
             store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
         }
+        else {
+            // fewer radial orders (a kmax cut, nmax < 128): their ceil(nmax / 2) row pairs
+            // spread evenly over the 16 warps (the rows past the count stay zero)
+            const int npr = (nmax + 1) >> 1;
+            const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
+            const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
+            const float2 w2 = make_float2(pt.w, pt.w);
+            for (int jp = jp0; jp < jp1; ++jp) {
+                const int n = 2 * jp;
+                const float4 kk = s_kzp[jp];
+                const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
+                const float2 p = __fmul2_rn(rh2, kx);
+                float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
+                e = __ffma2_rn(rh2, ky, e);
+                e = __ffma2_rn(rl2, kx, e);
+                const float2 fl = make_float2(rintf(p.x), rintf(p.y));
+                const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);
+                const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
+                const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
+                const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
+                float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
+                ja = fmaf(ja, uu.x, a1.x);
+                jb = fmaf(jb, uu.y, b1.x);
+                ja = fmaf(ja, uu.x, a0.w);
+                jb = fmaf(jb, uu.y, b0.w);
+                ja = fmaf(ja, uu.x, a0.z);
+                jb = fmaf(jb, uu.y, b0.z);
+                ja = fmaf(ja, uu.x, a0.y);
+                jb = fmaf(jb, uu.y, b0.y);
+                ja = fmaf(ja, uu.x, a0.x);
+                jb = fmaf(jb, uu.y, b0.x);
+                const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
+                const float2 v = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
+                __half2 hh = __float22half2_rn(v);
+                const float2 hf = __half22float2(hh);
+                __half2 ll = __float22half2_rn(__fadd2_rn(v, make_float2(-hf.x, -hf.y)));
+                const uint32_t off = tc05::mn_sw128_off(n, q, 2);
+                *reinterpret_cast<__half2 *>(jhi + off) = hh;
+                *reinterpret_cast<__half2 *>(jlo + off) = ll;
+            }
+        }
         // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
         if (mlo < mhi) {
             const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
@@ -488,22 +547,55 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
                     {
                         const int m = mb0 + ml;
                         float2 P;
-                        if (!EXT && m + 1 <= l - 2 && ml + 1 < mcount) {
+                        if (m + 1 <= l - 2 && ml + 1 < mcount) {
                             // both m take the plain three-term step: packed arithmetic
                             const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
                             const float2 p1 = make_float2(stg1[ml * KT + q], stg1[(ml + 1) * KT + q]);
-                            const float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
+                            float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
+                            unsigned ea = 0, eb = 0;  // extended range: exponents of P_{l-1} at m, m+1
+                            if (EXT) {
+                                ea = ebits(stge1[ml], q);
+                                eb = ebits(stge1[ml + 1], q);
+                                const unsigned fa = ebits(stge2[ml], q), fb = ebits(stge2[ml + 1], q);
+                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                if (fa != ea) p2.x = (fa == ea + 1) ? p2.x * 0x1p-64f * 0x1p-64f : 0.f;
+                                if (fb != eb) p2.y = (fb == eb + 1) ? p2.y * 0x1p-64f * 0x1p-64f : 0.f;
+                            }
                             const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
                             const float2 bb =
                                 __ffma2_rn(make_float2(cb.z, cb.w), p2, __fmul2_rn(make_float2(cb.x, cb.y), p2));
                             const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
                             P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                            if (EXT) {  // renormalise values that grew past 2^40 while e > 0
+                                if (ea > 0 && fabsf(P.x) > 0x1p40f) {
+                                    P.x = P.x * 0x1p-64f * 0x1p-64f;
+                                    --ea;
+                                }
+                                if (eb > 0 && fabsf(P.y) > 0x1p40f) {
+                                    P.y = P.y * 0x1p-64f * 0x1p-64f;
+                                    --eb;
+                                }
+                            }
                             if (wrows) {
                                 rowp[0] = P.x;
                                 rowp[stride] = P.y;
                             }
+                            if (EXT && wrows) {
+                                const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
+                                const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
+                                const unsigned b0 = __ballot_sync(0xffffffffu, eb & 1u);
+                                const unsigned b1 = __ballot_sync(0xffffffffu, (eb >> 1) & 1u);
+                                if (lane == 0) {
+                                    ex0[t * cat.epitch + m] = ((unsigned long long)a1 << 32) | a0;
+                                    ex0[t * cat.epitch + m + 1] = ((unsigned long long)b1 << 32) | b0;
+                                }
+                            }
+                            if (EXT) {  // values with e > 0 are below 2^-188: no contribution
+                                if (ea) P.x = 0.f;
+                                if (eb) P.y = 0.f;
+                            }
                         } else {
-                            // sectoral (m = l), m = l - 1, the block's last odd m, or extended range
+                            // sectoral (m = l), m = l - 1, or the block's last odd m
                             const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
                             float pv[2];
 #pragma unroll
@@ -971,8 +1063,14 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     if (cats.empty()) return CATANA_OK;
     static bool attr = false;
     if (!attr) {
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES));
         attr = true;
     }
     // ---- extents: max r and max |w| per catalog (one synchronisation) ----
@@ -1062,7 +1160,12 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int lmax_g = 0;
         for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
-        auto kern = ext ? k_split_l<true> : k_split_l<false>;
+        // kernel per level: extended-range rows above lmax 256; the full-J layout when every
+        // item of the level has 128 radial orders in its half
+        auto kern_for = [&](bool full) {
+            return ext ? (full ? k_split_l<true, true> : k_split_l<true, false>)
+                       : (full ? k_split_l<false, true> : k_split_l<false, false>);
+        };
         // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
         size_t ws_bytes = 0;
@@ -1195,6 +1298,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             std::vector<SplitItem> items;
             std::vector<SplitRed> reds;
             std::vector<int> item0, red0, maxn;
+            std::vector<char> fullj;  // per level: every item has 128 radial orders in its half
             std::vector<double> flops;
         };
         auto schedule = [&](double waves, Sched &S) {
@@ -1203,6 +1307,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             S.item0.assign(lmax_g + 1, 0);
             S.red0.assign(lmax_g + 1, 0);
             S.maxn.assign(lmax_g, 0);
+            S.fullj.assign(lmax_g, 1);
             S.flops.assign(lmax_g, 0.0);
             for (int l = 0; l < lmax_g; ++l) {
                 S.item0[l] = (int)S.items.size();
@@ -1264,6 +1369,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                                 it.mb0 = mb0;
                                 it.mcount = std::min(mblk, l + 1 - mb0);
                                 it.n0 = hf * NHALF;
+                                if (std::min(NHALF, P.nmax_l[l] - it.n0) < NHALF) S.fullj[l] = 0;
                                 it.t0 = (int64_t)sl * Tc;
                                 it.t1 = std::min<int64_t>(P.ntiles, it.t0 + Tc);
                                 S.items.push_back(it);
@@ -1339,7 +1445,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                             if (l >= lmax_g) continue;
                             const int ni = S.item0[l + 1] - S.item0[l];
                             if (ni == 0) continue;
-                            kern<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
+                            kern_for(S.fullj[l] != 0)<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
                             count_launch();
                         }
                         CG_CUDA_TRY(cudaGetLastError());
@@ -1370,7 +1476,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const int nr = S.red0[l + 1] - S.red0[l];
                 if (ni == 0) continue;
                 if (profile) prof_begin(ls_st);
-                kern<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
+                kern_for(S.fullj[l] != 0)<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
                 if (profile) prof_end(ls_st, S.flops[l]);
                 dim3 rg(ceil_div((int64_t)(l + 1) * S.maxn[l], 128), nr);
                 k_split_reduce<<<rg, 128, 0, ls_st>>>(partial, l + 1,
