@@ -20,8 +20,13 @@
 //               partial sums [ring][m][n]
 //   k_hp_reduce sum over rings in ring order; C_ln = (2 sum_m |f|^2 - |f_0|^2)
 //               (norm k)^2 / (2l+1) and f stored as f k norm (sfb_reverse_fft.cpp:147-153)
-// The ring transform is a direct DFT of only the needed frequencies, evaluated as a
-// small GEMM per ring (map chunk and twiddles staged in shared memory).
+// The ring transform: rings whose length is a power of two (all equatorial rings when
+// nside is one, and the polar rings of 4, 8, 16, ... pixels) take a batched FP64 FFT
+// (k_hp_fft: two radial orders packed as one complex sequence, radix-4 passes in
+// shared memory) once l is large enough that the FFT's n log n beats the direct sum's
+// n (l + 1); the other rings take a direct DFT of only the needed frequencies, a small
+// GEMM per ring (map chunk and twiddles staged in shared memory).  Both end in the same
+// m-extraction and the same per-ring partial sums.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -139,6 +144,7 @@ constexpr int HP_MAXPIX = 4096;  // twiddle table capacity (ring length, 4 nside
 
 // per ring: G(m, n) = F_ring[s(m)](n) with the reference's extraction, times Y_lm(ring)
 __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restrict__ map, int nmax, int l,
+                                                         const int *__restrict__ rings,
                                                          const int64_t *__restrict__ ring_start,
                                                          const int *__restrict__ ring_pix,
                                                          const double2 *__restrict__ tw_all,
@@ -148,7 +154,7 @@ __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restri
     extern __shared__ double hp_smem[];
     double2 *s_tw = reinterpret_cast<double2 *>(hp_smem);          // [rpix]
     double *s_map = hp_smem + 2 * HP_MAXPIX;                        // [HP_JC][HP_NB]
-    const int r = blockIdx.x;
+    const int r = rings[blockIdx.x];
     const int n0 = blockIdx.y * HP_NB, m0 = blockIdx.z * (HP_MS * HP_MPT);
     const int rpix = ring_pix[r];
     const int64_t rs = ring_start[r];
@@ -205,6 +211,106 @@ __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restri
     }
 }
 
+constexpr int HF_G = 2;    // complex sequences (radial-order pairs) per CTA
+constexpr int HF_T = 256;  // threads per CTA
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
+// Power-of-two ring of N pixels: the complex sequence z_j = map_j(n) + i map_j(n + 1)
+// (two radial orders) goes through an in-place decimation-in-time FFT, loaded in
+// bit-reversed order, radix-4 passes (each two radix-2 stages of half-lengths h and 2h,
+// the second pair's twiddle W_4h^(j+h) = -i W_4h^j) and one radix-2 pass when log2 N is
+// odd.  The two real transforms are A[s] = (Z[s] + conj Z[N-s]) / 2 and
+// B[s] = (Z[s] - conj Z[N-s]) / 2i; the m-extraction, the sign rules and the product
+// with Y_lm(ring) are those of k_hp_ring.
+__global__ void __launch_bounds__(HF_T) k_hp_fft(const double *__restrict__ map, int nmax, int l,
+                                                const int *__restrict__ rings,
+                                                const int64_t *__restrict__ ring_start,
+                                                const int *__restrict__ ring_pix,
+                                                const double2 *__restrict__ tw_all,
+                                                const int64_t *__restrict__ tw_off,
+                                                const double2 *__restrict__ ylm, int conj_fix,
+                                                double2 *__restrict__ partial /* [ring][m][n] */) {
+    extern __shared__ double2 hf_x[];  // [HF_G][N]
+    const int r = rings[blockIdx.x];
+    const int N = ring_pix[r], logn = __ffs(N) - 1;
+    const int64_t rs = ring_start[r];
+    const double2 *__restrict__ tw = tw_all + tw_off[r];  // tw[k] = e^{-2 pi i k / N}
+    const int q0 = blockIdx.y * HF_G, tid = threadIdx.x;
+    // map columns n = 2 q0 .. 2 q0 + 2 HF_G - 1 of the ring's pixels, bit-reversed
+    for (int e = tid; e < N * 2 * HF_G; e += HF_T) {
+        const int j = e / (2 * HF_G), t = e - j * (2 * HF_G);
+        const int n = 2 * q0 + t;
+        const double v = n < nmax ? __ldg(map + (rs + j) * nmax + n) : 0.0;
+        const int jr = logn ? (int)(__brev((unsigned)j) >> (32 - logn)) : 0;
+        reinterpret_cast<double *>(hf_x + (t >> 1) * N + jr)[t & 1] = v;
+    }
+    const int nb4 = N >> 2;
+    int h = 1;
+    for (; 4 * h <= N; h *= 4) {
+        __syncthreads();
+        for (int e = tid; e < HF_G * nb4; e += HF_T) {
+            const int g = e >> (logn - 2), k = e & (nb4 - 1);
+            const int j = k & (h - 1);
+            double2 *xs = hf_x + g * N + ((k - j) << 2) + j;
+            double2 x0 = xs[0], x1 = xs[h], x2 = xs[2 * h], x3 = xs[3 * h];
+            if (h > 1) {
+                const double2 w2 = __ldg(tw + j * (N / (2 * h)));
+                x1 = cmul(x1, w2);
+                x3 = cmul(x3, w2);
+            }
+            double2 y0 = make_double2(x0.x + x1.x, x0.y + x1.y), y1 = make_double2(x0.x - x1.x, x0.y - x1.y);
+            double2 y2 = make_double2(x2.x + x3.x, x2.y + x3.y), y3 = make_double2(x2.x - x3.x, x2.y - x3.y);
+            if (h > 1) {
+                const double2 w4 = __ldg(tw + j * (N / (4 * h)));
+                y2 = cmul(y2, w4);
+                y3 = cmul(y3, w4);
+            }
+            y3 = make_double2(y3.y, -y3.x);  // times -i
+            xs[0] = make_double2(y0.x + y2.x, y0.y + y2.y);
+            xs[2 * h] = make_double2(y0.x - y2.x, y0.y - y2.y);
+            xs[h] = make_double2(y1.x + y3.x, y1.y + y3.y);
+            xs[3 * h] = make_double2(y1.x - y3.x, y1.y - y3.y);
+        }
+    }
+    if (h < N) {  // N = 2 h: the last radix-2 stage
+        __syncthreads();
+        const int nb2 = N >> 1;
+        for (int e = tid; e < HF_G * nb2; e += HF_T) {
+            const int g = e >> (logn - 1), j = e & (nb2 - 1);
+            double2 *xs = hf_x + g * N + j;
+            const double2 u = xs[0], v = cmul(xs[h], __ldg(tw + j));
+            xs[0] = make_double2(u.x + v.x, u.y + v.y);
+            xs[h] = make_double2(u.x - v.x, u.y - v.y);
+        }
+    }
+    __syncthreads();
+    const int half = N >> 1;
+    for (int e = tid; e < (l + 1) * HF_G; e += HF_T) {
+        const int m = e / HF_G, g = e - m * HF_G;
+        const int n = 2 * (q0 + g);
+        if (n >= nmax) continue;
+        const int mm = m & (N - 1);
+        const int d = half - mm;
+        const int s = half - (d < 0 ? -d : d);
+        const double2 zs = hf_x[g * N + s], zn = hf_x[g * N + ((N - s) & (N - 1))];
+        double ar = zs.x + zn.x, ai = zs.y - zn.y;  // 2 A[s]
+        double br = zs.y + zn.y, bi = zn.x - zs.x;  // 2 B[s]
+        if (m == 0) ai = bi = 0.0;                  // sign = 0 at m = 0
+        if (conj_fix && 2 * mm > N) {               // the alias is the conjugate
+            ai = -ai;
+            bi = -bi;
+        }
+        const double2 y = ylm[(size_t)r * (l + 1) + m];
+        const double yr = 0.5 * y.x, yi = 0.5 * y.y;
+        double2 *out = partial + ((size_t)r * (l + 1) + m) * nmax + n;
+        out[0] = make_double2(ar * yr - ai * yi, ar * yi + ai * yr);
+        if (n + 1 < nmax) out[1] = make_double2(br * yr - bi * yi, br * yi + bi * yr);
+    }
+}
+
 // f(m, n) = sum over rings (ring order), stored as f k norm (sfb_reverse_fft.cpp:152-153)
 __global__ void k_hp_reduce(const double2 *__restrict__ partial, int nrings, int l, int nmax,
                             const double *__restrict__ kln, double norm, double2 *__restrict__ fl) {
@@ -239,8 +345,20 @@ struct RingTables {
     int64_t nside = -1;
     int nrings = 0;
     DevBuf buf;
-    size_t off_start = 0, off_pix = 0, off_x = 0, off_phi = 0, off_tw = 0, off_twoff = 0;
+    size_t off_start = 0, off_pix = 0, off_x = 0, off_phi = 0, off_tw = 0, off_twoff = 0, off_order = 0;
+    // ring order: power-of-two rings by increasing length, then the others; the rings
+    // taking the FFT at multipole l are the prefix of fft_count[l] entries
+    int max_pow2 = 0;                // longest power-of-two ring
+    std::vector<int> pow2_log;       // log2 length of the power-of-two rings, in order
 };
+
+// the FFT (about 1.8 N log2 N FP64 operations per radial order) beats the direct sum
+// (2 N (l + 1)) from l + 1 >= log2 N + 2 on
+int fft_count(const RingTables &R, int l) {
+    int c = 0;
+    while (c < (int)R.pow2_log.size() && l + 1 >= R.pow2_log[c] + 2) ++c;
+    return c;
+}
 RingTables g_rings;
 
 // host copies of the HEALPix ring geometry (same formulas as the device functions)
@@ -335,13 +453,31 @@ catana_status_t ensure_rings(int64_t nside, cudaStream_t st) {
         x[r] = std::cos(th);  // RingInfo: cos(theta) of the first pixel (sfb_reverse_fft.cpp:21)
         ph[r] = phi;
     }
+    std::vector<int> order(nrings);
+    for (int r = 0; r < nrings; ++r) order[r] = r;
+    auto is_pow2 = [&](int r) { return (rp[r] & (rp[r] - 1)) == 0; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const bool pa = is_pow2(a), pb = is_pow2(b);
+        if (pa != pb) return pa;
+        return pa && rp[a] < rp[b];
+    });
+    R.pow2_log.clear();
+    R.max_pow2 = 0;
+    for (int r : order) {
+        if (!is_pow2(r)) break;
+        int lg = 0;
+        while ((1 << lg) < rp[r]) ++lg;
+        R.pow2_log.push_back(lg);
+        R.max_pow2 = std::max(R.max_pow2, rp[r]);
+    }
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     R.off_start = 0;
     R.off_pix = al(R.off_start + nrings * sizeof(int64_t));
     R.off_x = al(R.off_pix + nrings * sizeof(int));
     R.off_phi = al(R.off_x + nrings * sizeof(double));
     R.off_twoff = al(R.off_phi + nrings * sizeof(double));
-    R.off_tw = al(R.off_twoff + nrings * sizeof(int64_t));
+    R.off_order = al(R.off_twoff + nrings * sizeof(int64_t));
+    R.off_tw = al(R.off_order + nrings * sizeof(int));
     const size_t total = R.off_tw + tw.size() * sizeof(double2);
     CG_CUDA_TRY(R.buf.ensure(total));
     char *b = R.buf.as<char>();
@@ -350,6 +486,7 @@ catana_status_t ensure_rings(int64_t nside, cudaStream_t st) {
     CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_x, x.data(), nrings * sizeof(double), cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_phi, ph.data(), nrings * sizeof(double), cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_twoff, twoff.data(), nrings * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_order, order.data(), nrings * sizeof(int), cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemcpyAsync(b + R.off_tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaStreamSynchronize(st));
     R.nside = nside;
@@ -442,6 +579,7 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
     const double *ring_phi = reinterpret_cast<const double *>(rb + R.off_phi);
     const int64_t *tw_off = reinterpret_cast<const int64_t *>(rb + R.off_twoff);
     const double2 *tw = reinterpret_cast<const double2 *>(rb + R.off_tw);
+    const int *order = reinterpret_cast<const int *>(rb + R.off_order);
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t mapb = al((size_t)npix * nmax * sizeof(double));
     const size_t ylmb = al((size_t)nrings * lmax * sizeof(double2));
@@ -452,9 +590,12 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
     double2 *partial = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb + ylmb);
     const int npts_tab = 1000 * nmax;
     const size_t smem = (2 * HP_MAXPIX + HP_JC * HP_NB) * sizeof(double);
+    const size_t smem_fft = (size_t)HF_G * R.max_pow2 * sizeof(double2);
     static bool attr = false;
     if (!attr) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_hp_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CG_CUDA_TRY(cudaFuncSetAttribute(k_hp_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(HF_G * HP_MAXPIX * sizeof(double2))));
         attr = true;
     }
     for (int l = 0; l < lmax; ++l) {
@@ -464,16 +605,26 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
             interpolated ? ctx->tab_dxinv[l] : 0.0, interpolated ? ctx->tab_zmax[l] : 0.0, l, map, err_dev);
         k_hp_ylm<<<ceil_div(nrings * (l + 1), 128), 128, 0, st>>>(ring_x, ring_phi, nrings, l, ctx->coef.as<double2>(),
                                                                   ylm);
-        dim3 grid(nrings, ceil_div(nmax, HP_NB), ceil_div(l + 1, HP_MS * HP_MPT));
+        const int nfft = fft_count(R, l);
         prof_begin(st);
-        k_hp_ring<<<grid, HP_NB * HP_MS, smem, st>>>(map, nmax, l, ring_start, ring_pix, tw, tw_off, ylm,
-                                                     conj_fix ? 1 : 0, partial);
+        if (nfft > 0) {
+            dim3 gf(nfft, ceil_div(ceil_div(nmax, 2), HF_G));
+            k_hp_fft<<<gf, HF_T, smem_fft, st>>>(map, nmax, l, order, ring_start, ring_pix, tw, tw_off, ylm,
+                                                 conj_fix ? 1 : 0, partial);
+            count_launch();
+        }
+        if (nfft < nrings) {
+            dim3 grid(nrings - nfft, ceil_div(nmax, HP_NB), ceil_div(l + 1, HP_MS * HP_MPT));
+            k_hp_ring<<<grid, HP_NB * HP_MS, smem, st>>>(map, nmax, l, order + nfft, ring_start, ring_pix, tw,
+                                                         tw_off, ylm, conj_fix ? 1 : 0, partial);
+            count_launch();
+        }
         prof_end(st, 4.0 * (double)npix * nmax * (l + 1));
         double2 *fl = reinterpret_cast<double2 *>(f_dev) + (size_t)nmax * l * (l + 1) / 2;
         k_hp_reduce<<<ceil_div((l + 1) * nmax, 128), 128, 0, st>>>(partial, nrings, l, nmax,
                                                                    kln_dev + (size_t)l * nmax, norm, fl);
         k_hp_cln<<<ceil_div(nmax, 64), 64, 0, st>>>(fl, l, nmax, c_ln_dev + (size_t)l * nmax);
-        count_launch(5);
+        count_launch(4);
         CG_CUDA_TRY(cudaGetLastError());
     }
     return CATANA_OK;

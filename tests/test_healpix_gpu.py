@@ -87,9 +87,13 @@ def test_golden_healpix(cuda_device, golden):
     _compare(res, k, c, f)
 
 
-@pytest.mark.parametrize("nside,n,lmax,nmax", [(8, 3000, 40, 12), (16, 1500, 20, 10), (32, 5000, 16, 40)])
+@pytest.mark.parametrize("nside,n,lmax,nmax", [(8, 3000, 40, 12), (16, 1500, 20, 10), (32, 5000, 16, 40),
+                                                (64, 20000, 30, 17)])
 def test_healpix_vs_oracle(cuda_device, nside, n, lmax, nmax):
-    """Polar rings shorter than 2l exercise the reference's unconjugated alias."""
+    """Polar rings shorter than 2l exercise the reference's unconjugated alias.  Rings of
+    power-of-two length go through the FFT once l + 1 >= log2(length) + 2 (every case
+    here reaches it: 32- to 256-pixel rings, both packed radial orders, an odd nmax);
+    the others through the direct ring sum."""
     pts = uniform_ball(n, 500.0, seed=nside)
     ppc = catana.PixelizedPointContainer(nside, catana.PointContainer(pts))
     res = catana.sfb_decomposition(ppc, lmax, nmax, 500.0, True, False)
