@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="skip e2e/cpu/plain/accuracy legs")
     p.add_argument("--stream-chunks", type=int, default=2,
                    help="8M-point chunks of the streamed lmax 512 / nmax 256 survey leg (0 skips it)")
+    p.add_argument("--only", default=None, choices=["side", "batched", "streamed", "next"],
+                   help="time one secondary workload alone (side: FP64 100k and HEALPix nside 256) and print "
+                        "its JSON")
     return p.parse_args()
 
 
@@ -498,6 +501,14 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if a.only is not None:
+        sp0 = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        run_one = {"side": lambda: side_workloads(torch, _lib, catana, sp0),
+                   "batched": lambda: batched_workload(torch, _lib, catana, sp0),
+                   "streamed": lambda: streamed_workload(torch, _lib, catana, chunks=max(1, a.stream_chunks)),
+                   "next": lambda: next_rows_workload(torch, _lib, catana)}[a.only]
+        print(json.dumps({"only": a.only, "result": run_one()}, default=float))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

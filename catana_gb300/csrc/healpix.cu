@@ -23,10 +23,10 @@
 // The ring transform: rings whose length is a power of two (all equatorial rings when
 // nside is one, and the polar rings of 4, 8, 16, ... pixels) take a batched FP64 FFT
 // (k_hp_fft: two radial orders packed as one complex sequence, radix-4 passes in
-// shared memory) once l is large enough that the FFT's n log n beats the direct sum's
-// n (l + 1); the other rings take a direct DFT of only the needed frequencies, a small
-// GEMM per ring (map chunk and twiddles staged in shared memory).  Both end in the same
-// m-extraction and the same per-ring partial sums.
+// shared memory) once l is large enough that the FFT's N log N beats the direct sum;
+// the other rings take a direct DFT of only the needed frequencies over the ring's
+// quarter-orbits (N/4 + 1 folded terms per frequency, folded chunks and twiddles staged
+// in shared memory).  Both end in the same m-extraction and per-ring partial sums.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -139,10 +139,18 @@ __global__ void k_hp_ylm(const double *__restrict__ ring_x, const double *__rest
 constexpr int HP_NB = 32;     // n per CTA
 constexpr int HP_MS = 8;      // m slots (threads) per n
 constexpr int HP_MPT = 8;     // m per thread -> 64 m per CTA
-constexpr int HP_JC = 64;     // pixels per staged map chunk
+constexpr int HP_JC = 32;     // folded quarter-ring positions per staged chunk
 constexpr int HP_MAXPIX = 4096;  // twiddle table capacity (ring length, 4 nside <= 4096)
 
-// per ring: G(m, n) = F_ring[s(m)](n) with the reference's extraction, times Y_lm(ring)
+// per ring: G(m, n) = F_ring[s(m)](n) with the reference's extraction, times Y_lm(ring).
+// A ring of N = 4 i pixels is real, so the pixels j, N-j, N/2-j, N/2+j share |cos| and
+// |sin| of 2 pi j s / N: with a = x_j + x_{N-j}, b = x_{N/2-j} + x_{N/2+j},
+// c = x_j - x_{N-j}, d = x_{N/2+j} - x_{N/2-j},
+//   Re F[s] = sum_{j=0}^{N/4} cos(2 pi j s / N) (a + (-1)^s b)
+//   Im F[s] = -sum_{j=0}^{N/4} sin(2 pi j s / N) (c + (-1)^s d)
+// (j = 0: a + b -> x_0 + (-1)^s x_{N/2}, no sine; j = N/4: the orbit {N/4, 3N/4}), so
+// the sum over N pixels becomes N/4 + 1 terms, folded once per chunk and shared by
+// every frequency of the CTA.
 __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restrict__ map, int nmax, int l,
                                                          const int *__restrict__ rings,
                                                          const int64_t *__restrict__ ring_start,
@@ -153,10 +161,10 @@ __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restri
                                                          double2 *__restrict__ partial /* [ring][m][n] */) {
     extern __shared__ double hp_smem[];
     double2 *s_tw = reinterpret_cast<double2 *>(hp_smem);          // [rpix]
-    double *s_map = hp_smem + 2 * HP_MAXPIX;                        // [HP_JC][HP_NB]
+    double *s_fold = hp_smem + 2 * HP_MAXPIX;                       // [4][HP_JC][HP_NB]: even/odd cos, even/odd sin
     const int r = rings[blockIdx.x];
     const int n0 = blockIdx.y * HP_NB, m0 = blockIdx.z * (HP_MS * HP_MPT);
-    const int rpix = ring_pix[r];
+    const int rpix = ring_pix[r], quarter = rpix >> 2, halfp = rpix >> 1;
     const int64_t rs = ring_start[r];
     const int tid = threadIdx.x, nl = tid % HP_NB, ms = tid / HP_NB;
     const int n = n0 + nl;
@@ -175,22 +183,49 @@ __global__ void __launch_bounds__(HP_NB *HP_MS) k_hp_ring(const double *__restri
         cur[k] = 0;
         gr[k] = gi[k] = 0.0;
     }
-    for (int j0 = 0; j0 < rpix; j0 += HP_JC) {
-        const int jn = min(HP_JC, rpix - j0);
+    for (int j0 = 0; j0 <= quarter; j0 += HP_JC) {
+        const int jn = min(HP_JC, quarter + 1 - j0);
         __syncthreads();
         for (int e = tid; e < HP_JC * HP_NB; e += blockDim.x) {
-            const int jj = e / HP_NB, nn = e % HP_NB;
-            s_map[e] = (jj < jn && n0 + nn < nmax) ? map[(rs + j0 + jj) * nmax + n0 + nn] : 0.0;
+            const int jj = e / HP_NB, nn = e % HP_NB, j = j0 + jj;
+            double ce = 0.0, co = 0.0, se = 0.0, so = 0.0;
+            if (jj < jn && n0 + nn < nmax) {
+                const double *col = map + rs * nmax + n0 + nn;
+                if (j == 0) {
+                    const double x0 = col[0], xh = col[(int64_t)halfp * nmax];
+                    ce = x0 + xh;
+                    co = x0 - xh;
+                } else if (j == quarter) {
+                    const double xa = col[(int64_t)quarter * nmax], xb = col[(int64_t)(3 * quarter) * nmax];
+                    ce = co = xa + xb;
+                    se = so = xa - xb;
+                } else {
+                    const double xj = col[(int64_t)j * nmax], xn = col[(int64_t)(rpix - j) * nmax];
+                    const double xm = col[(int64_t)(halfp - j) * nmax], xp = col[(int64_t)(halfp + j) * nmax];
+                    const double a = xj + xn, b = xm + xp, c = xj - xn, d = xp - xm;
+                    ce = a + b;
+                    co = a - b;
+                    se = c + d;
+                    so = c - d;
+                }
+            }
+            s_fold[e] = ce;
+            s_fold[HP_JC * HP_NB + e] = co;
+            s_fold[2 * HP_JC * HP_NB + e] = se;
+            s_fold[3 * HP_JC * HP_NB + e] = so;
         }
         __syncthreads();
         for (int jj = 0; jj < jn; ++jj) {
-            const double v = s_map[jj * HP_NB + nl];
+            const int o = jj * HP_NB + nl;
+            const double ce = s_fold[o], co = s_fold[HP_JC * HP_NB + o];
+            const double se = s_fold[2 * HP_JC * HP_NB + o], so = s_fold[3 * HP_JC * HP_NB + o];
 #pragma unroll
             for (int k = 0; k < HP_MPT; ++k) {
                 if (k < kval) {
-                    const double2 w = s_tw[cur[k]];
-                    gr[k] = fma(v, w.x, gr[k]);
-                    gi[k] = fma(v, w.y, gi[k]);
+                    const double2 w = s_tw[cur[k]];  // (cos, -sin) of 2 pi j s / N
+                    const bool odd = sidx[k] & 1;
+                    gr[k] = fma(odd ? co : ce, w.x, gr[k]);
+                    gi[k] = fma(odd ? so : se, w.y, gi[k]);
                     const int c = cur[k] + sidx[k];
                     cur[k] = c >= rpix ? c - rpix : c;
                 }
@@ -352,11 +387,11 @@ struct RingTables {
     std::vector<int> pow2_log;       // log2 length of the power-of-two rings, in order
 };
 
-// the FFT (about 1.8 N log2 N FP64 operations per radial order) beats the direct sum
-// (2 N (l + 1)) from l + 1 >= log2 N + 2 on
+// the FFT (about 2 N log2 N FP64 operations per radial order, measured) beats the folded
+// direct sum (N/2 (l + 1) + 2 N) from l + 1 > 4 log2 N - 4 on
 int fft_count(const RingTables &R, int l) {
     int c = 0;
-    while (c < (int)R.pow2_log.size() && l + 1 >= R.pow2_log[c] + 2) ++c;
+    while (c < (int)R.pow2_log.size() && l + 1 > 4 * R.pow2_log[c] - 4) ++c;
     return c;
 }
 RingTables g_rings;
@@ -589,7 +624,7 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
     double2 *ylm = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb);
     double2 *partial = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb + ylmb);
     const int npts_tab = 1000 * nmax;
-    const size_t smem = (2 * HP_MAXPIX + HP_JC * HP_NB) * sizeof(double);
+    const size_t smem = (2 * HP_MAXPIX + 4 * HP_JC * HP_NB) * sizeof(double);
     const size_t smem_fft = (size_t)HF_G * R.max_pow2 * sizeof(double2);
     static bool attr = false;
     if (!attr) {
