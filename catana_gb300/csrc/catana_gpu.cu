@@ -816,8 +816,19 @@ catana_status_t catana_gpu_sfb_healpix(int64_t nside, const int64_t *pix_offsets
     CG_CUDA_TRY(cudaMemcpyAsync(kln_d, kh.data(), lm * sizeof(double), cudaMemcpyHostToDevice, st));
     CG_CUDA_TRY(cudaMemsetAsync(f_d, 0, fc * 2 * sizeof(double), st));
     const double nf = norm_factor(rmax, (double)npoints);
+    double r_lo = 0.0, r_hi = 0.0;  // range of the radii; r_lo NaN when any radius is NaN
+    for (int64_t i = 0; i < npoints; ++i) {
+        const double r = r_sorted[i];
+        if (std::isnan(r)) {
+            r_lo = NAN;
+            break;
+        }
+        if (i == 0 || r < r_lo) r_lo = r;
+        if (i == 0 || r > r_hi) r_hi = r;
+    }
     s = healpix_sfb_dev(ctx, nside, off_d, rs_d, npoints, lmax, nmax, resolve_interp(flags, npoints),
-                        (flags & CATANA_HEALPIX_CONJ_FIX) != 0, kln_d, nf, f_d, cln_d, err_d, st);
+                        (flags & CATANA_HEALPIX_CONJ_FIX) != 0, kln_d, kh.data(), r_lo, r_hi, nf, f_d, cln_d, err_d,
+                        st);
     if (s != CATANA_OK) return s;
     int err_h = 0;
     CG_CUDA_TRY(cudaMemcpyAsync(&err_h, err_d, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -162,9 +162,12 @@ catana_status_t healpix_ang2pix_dev(int64_t nside, const double *theta, const do
                                     int64_t *pix, int *err_dev, cudaStream_t st);
 catana_status_t healpix_pix2ang_dev(int64_t nside, const int64_t *pix, int64_t n, double *theta, double *phi,
                                     cudaStream_t st);
+// kln_host (L x M, may be null) and the radii's range [r_min, r_max] (r_min NaN when a
+// radius is NaN) let levels that lie inside the j_l table skip the per-point range test
 catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t *offsets_dev,
                                 const double *r_sorted_dev, int64_t npoints, int lmax, int nmax, bool interpolated,
-                                bool conj_fix, const double *kln_dev, double norm, double *f_dev, double *c_ln_dev,
-                                int *err_dev, cudaStream_t st);
+                                bool conj_fix, const double *kln_dev, const double *kln_host, double r_min,
+                                double r_max, double norm, double *f_dev, double *c_ln_dev, int *err_dev,
+                                cudaStream_t st);
 
 }  // namespace catana_gpu

@@ -78,7 +78,13 @@ __global__ void k_bin_gather(const double *pts, const uint32_t *perm, int64_t n,
     if (i <= npix) offs[i] = (i == npix) ? n : (int64_t)offs32[i];
 }
 
-// map[pix][n] = sum over the pixel's points (in order) of j_l(k_ln r)
+// map[pix][n] = sum over the pixel's points (in order) of j_l(k_ln r).  CHECKED: every
+// argument k r is tested against the table's range [0, zmax) (a domain error otherwise);
+// unchecked launches are made only when the host has shown that the whole level lies in
+// range (0 <= r_min and k_max r_max < zmax, the same FP64 product as here), and form the
+// table position as r (k / dx) -- one rounding away from (k r) / dx, a change of the
+// interpolated value far below 1e-10 of the table's scale.
+template <bool CHECKED>
 __global__ void k_hp_map(const int64_t *__restrict__ offs, const double *__restrict__ r, int64_t npix, int nmax,
                          const double *__restrict__ kln, const double *__restrict__ tab, int npts_tab, double dx_inv,
                          double zmax, int l, double *__restrict__ map, int *err) {
@@ -87,22 +93,28 @@ __global__ void k_hp_map(const int64_t *__restrict__ offs, const double *__restr
     const int64_t pix = t / nmax;
     const int n = (int)(t - pix * nmax);
     const double k = kln[n];
+    const double kd = k * dx_inv;
     double s = 0.0;
     for (int64_t q = offs[pix]; q < offs[pix + 1]; ++q) {
-        const double z = k * r[q];
         double j;
         if (tab) {
-            if (!(z >= 0.0) || z >= zmax) {
-                *err = CATANA_ERR_DOMAIN;
-                j = 0.0;
+            double ia;
+            if (CHECKED) {
+                const double z = k * r[q];
+                if (!(z >= 0.0) || z >= zmax) {
+                    *err = CATANA_ERR_DOMAIN;
+                    ia = 0.0;
+                } else {
+                    ia = z * dx_inv;
+                }
             } else {
-                const double ia = z * dx_inv;
-                int ii = (int)ia;
-                if (ii > npts_tab - 2) ii = npts_tab - 2;
-                j = tab[ii] + (tab[ii + 1] - tab[ii]) * (ia - ii);
+                ia = r[q] * kd;
             }
+            int ii = (int)ia;
+            if (ii > npts_tab - 2) ii = npts_tab - 2;
+            j = tab[ii] + (tab[ii + 1] - tab[ii]) * (ia - ii);
         } else {
-            j = sbessel_jl(l, z);
+            j = sbessel_jl(l, k * r[q]);
         }
         s += j;
     }
@@ -589,8 +601,9 @@ catana_status_t healpix_bin_dev(DeviceContext *ctx, int64_t nside, const double 
 
 catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t *offsets_dev,
                                 const double *r_sorted_dev, int64_t npoints, int lmax, int nmax, bool interpolated,
-                                bool conj_fix, const double *kln_dev, double norm, double *f_dev, double *c_ln_dev,
-                                int *err_dev, cudaStream_t st) {
+                                bool conj_fix, const double *kln_dev, const double *kln_host, double r_min,
+                                double r_max, double norm, double *f_dev, double *c_ln_dev, int *err_dev,
+                                cudaStream_t st) {
     if (lmax == 0 || nmax == 0) return CATANA_OK;
     if (4 * nside > HP_MAXPIX) {
         set_error("HEALPix path supports nside <= 1024");
@@ -634,7 +647,11 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
         attr = true;
     }
     for (int l = 0; l < lmax; ++l) {
-        k_hp_map<<<ceil_div(npix * nmax, 256), 256, 0, st>>>(
+        // the level is in the table's range when 0 <= r_min and k_max r_max < zmax (NaN radii fail both)
+        const bool in_range = interpolated && kln_host && r_min >= 0.0 &&
+                              kln_host[(size_t)l * nmax + nmax - 1] * r_max < ctx->tab_zmax[l];
+        auto map_kern = in_range ? k_hp_map<false> : k_hp_map<true>;
+        map_kern<<<ceil_div(npix * nmax, 256), 256, 0, st>>>(
             offsets_dev, r_sorted_dev, npix, nmax, kln_dev + (size_t)l * nmax,
             interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr, npts_tab,
             interpolated ? ctx->tab_dxinv[l] : 0.0, interpolated ? ctx->tab_zmax[l] : 0.0, l, map, err_dev);
