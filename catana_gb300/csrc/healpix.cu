@@ -18,7 +18,7 @@
 //               m mod rpix > rpix/2 it uses F[rpix - m mod rpix] itself; the
 //               CATANA_HEALPIX_CONJ_FIX flag conjugates it.  Times Y_lm(ring) -> per-ring
 //               partial sums [ring][m][n]
-//   k_hp_reduce sum over rings in ring order; C_ln = (2 sum_m |f|^2 - |f_0|^2)
+//   k_hp_reduce sum over rings (interleaved per warp, fixed order); C_ln = (2 sum_m |f|^2 - |f_0|^2)
 //               (norm k)^2 / (2l+1) and f stored as f k norm (sfb_reverse_fft.cpp:147-153)
 // The ring transform: rings whose length is a power of two (all equatorial rings when
 // nside is one, and the polar rings of 4, 8, 16, ... pixels) take a batched FP64 FFT
@@ -359,19 +359,35 @@ __global__ void __launch_bounds__(HF_T) k_hp_fft(const double *__restrict__ map,
 }
 
 // f(m, n) = sum over rings (ring order), stored as f k norm (sfb_reverse_fft.cpp:152-153)
-__global__ void k_hp_reduce(const double2 *__restrict__ partial, int nrings, int l, int nmax,
-                            const double *__restrict__ kln, double norm, double2 *__restrict__ fl) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (l + 1) * nmax) return;
-    const int m = t / nmax, n = t - m * nmax;
+constexpr int HR_W = 8;  // warps per reduction block, each over every HR_W-th ring
+
+// CTA per (m, 32 radial orders): warp w sums rings w, w + HR_W, ... (lane = n), then
+// warp 0 adds the HR_W sums in warp order -- a fixed order, so repeated calls agree bit
+// for bit
+__global__ void __launch_bounds__(32 * HR_W) k_hp_reduce(const double2 *__restrict__ partial, int nrings, int l,
+                                                         int nmax, const double *__restrict__ kln, double norm,
+                                                         double2 *__restrict__ fl) {
+    __shared__ double2 s_sum[HR_W][32];
+    const int m = blockIdx.x, n = blockIdx.y * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
     double sr = 0.0, si = 0.0;
-    for (int r = 0; r < nrings; ++r) {
-        const double2 v = partial[((size_t)r * (l + 1) + m) * nmax + n];
-        sr += v.x;
-        si += v.y;
+    if (n < nmax) {
+        for (int r = w; r < nrings; r += HR_W) {
+            const double2 v = partial[((size_t)r * (l + 1) + m) * nmax + n];
+            sr += v.x;
+            si += v.y;
+        }
+    }
+    s_sum[w][threadIdx.x & 31] = make_double2(sr, si);
+    __syncthreads();
+    if (w != 0 || n >= nmax) return;
+    double tr = 0.0, ti = 0.0;
+#pragma unroll
+    for (int k = 0; k < HR_W; ++k) {
+        tr += s_sum[k][threadIdx.x].x;
+        ti += s_sum[k][threadIdx.x].y;
     }
     const double k = kln[n];
-    fl[t] = make_double2(sr * k * norm, si * k * norm);
+    fl[(size_t)m * nmax + n] = make_double2(tr * k * norm, ti * k * norm);
 }
 
 // C_ln = (2 sum_m |f|^2 - |f_0|^2) / (2l+1) of the stored f (sfb_reverse_fft.cpp:147-150)
@@ -673,7 +689,7 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
         }
         prof_end(st, 4.0 * (double)npix * nmax * (l + 1));
         double2 *fl = reinterpret_cast<double2 *>(f_dev) + (size_t)nmax * l * (l + 1) / 2;
-        k_hp_reduce<<<ceil_div((l + 1) * nmax, 128), 128, 0, st>>>(partial, nrings, l, nmax,
+        k_hp_reduce<<<dim3(l + 1, ceil_div(nmax, 32)), 32 * HR_W, 0, st>>>(partial, nrings, l, nmax,
                                                                    kln_dev + (size_t)l * nmax, norm, fl);
         k_hp_cln<<<ceil_div(nmax, 64), 64, 0, st>>>(fl, l, nmax, c_ln_dev + (size_t)l * nmax);
         count_launch(4);
