@@ -240,7 +240,7 @@ def side_workloads(torch, _lib, catana, sp):
     res["healpix_nside256_1M_l128_n64"] = {"binning_s": tb, "sfb_s": ts, "ring_transform_s": kms.value / 1e3,
                                            "note": "host API incl. copies; FP64; ring transform: batched FFT "
                                                    "for the power-of-two rings (the 513 equatorial rings of "
-                                                   "1024 pixels and 16 polar ones), direct DFT for the rest"}
+                                                   "1024 pixels and 16 polar ones), direct sums over quarter-orbits for the rest"}
     return res
 
 
