@@ -88,12 +88,14 @@ def test_golden_healpix(cuda_device, golden):
 
 
 @pytest.mark.parametrize("nside,n,lmax,nmax", [(8, 3000, 40, 12), (16, 1500, 20, 10), (32, 5000, 16, 40),
-                                                (64, 20000, 30, 17)])
+                                                (64, 20000, 30, 17), (4, 4000, 48, 9), (2, 1200, 20, 5),
+                                                (1, 1500, 12, 4)])
 def test_healpix_vs_oracle(cuda_device, nside, n, lmax, nmax):
     """Polar rings shorter than 2l exercise the reference's unconjugated alias.  Rings of
-    power-of-two length go through the FFT once l + 1 >= log2(length) + 2 (every case
-    here reaches it: 32- to 256-pixel rings, both packed radial orders, an odd nmax);
-    the others through the direct ring sum."""
+    power-of-two length go through the FFT once l + 1 > 4 log2(length) - 4 (equatorial
+    rings at nside 1 to 8 and 64, polar rings of 4 to 32 pixels; both packed radial
+    orders, odd nmax); the other polar rings (4 i pixels, i not a power of two: 12, 20,
+    24, 28, ...) through the folded direct sum.  nside 1: every ring has 4 pixels."""
     pts = uniform_ball(n, 500.0, seed=nside)
     ppc = catana.PixelizedPointContainer(nside, catana.PointContainer(pts))
     res = catana.sfb_decomposition(ppc, lmax, nmax, 500.0, True, False)
