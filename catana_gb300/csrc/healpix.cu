@@ -267,9 +267,9 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 
 // Power-of-two ring of N pixels: the complex sequence z_j = map_j(n) + i map_j(n + 1)
 // (two radial orders) goes through an in-place decimation-in-time FFT, loaded in
-// bit-reversed order, radix-4 passes (each two radix-2 stages of half-lengths h and 2h,
-// the second pair's twiddle W_4h^(j+h) = -i W_4h^j) and one radix-2 pass when log2 N is
-// odd.  The two real transforms are A[s] = (Z[s] + conj Z[N-s]) / 2 and
+// bit-reversed order, radix-4 passes (each two radix-2 stages of half-lengths h and 2h
+// fused into one butterfly: inputs 1, 2, 3 times W_4h^2j, W_4h^j, W_4h^3j, then sums with
+// +-1 and +-i) and one radix-2 pass when log2 N is odd.  The two real transforms are A[s] = (Z[s] + conj Z[N-s]) / 2 and
 // B[s] = (Z[s] - conj Z[N-s]) / 2i; the m-extraction, the sign rules and the product
 // with Y_lm(ring) are those of k_hp_ring.
 __global__ void __launch_bounds__(HF_T) k_hp_fft(const double *__restrict__ map, int nmax, int l,
@@ -302,24 +302,21 @@ __global__ void __launch_bounds__(HF_T) k_hp_fft(const double *__restrict__ map,
             const int g = e >> (logn - 2), k = e & (nb4 - 1);
             const int j = k & (h - 1);
             double2 *xs = hf_x + g * N + ((k - j) << 2) + j;
-            double2 x0 = xs[0], x1 = xs[h], x2 = xs[2 * h], x3 = xs[3 * h];
-            if (h > 1) {
-                const double2 w2 = __ldg(tw + j * (N / (2 * h)));
-                x1 = cmul(x1, w2);
-                x3 = cmul(x3, w2);
+            const double2 x0 = xs[0];
+            double2 t1 = xs[h], t2 = xs[2 * h], t3 = xs[3 * h];
+            if (h > 1) {  // t1 W^2j, t2 W^j, t3 W^3j with W = W_4h
+                const int st = N / (4 * h);
+                t1 = cmul(t1, __ldg(tw + 2 * j * st));
+                t2 = cmul(t2, __ldg(tw + j * st));
+                t3 = cmul(t3, __ldg(tw + 3 * j * st));
             }
-            double2 y0 = make_double2(x0.x + x1.x, x0.y + x1.y), y1 = make_double2(x0.x - x1.x, x0.y - x1.y);
-            double2 y2 = make_double2(x2.x + x3.x, x2.y + x3.y), y3 = make_double2(x2.x - x3.x, x2.y - x3.y);
-            if (h > 1) {
-                const double2 w4 = __ldg(tw + j * (N / (4 * h)));
-                y2 = cmul(y2, w4);
-                y3 = cmul(y3, w4);
-            }
-            y3 = make_double2(y3.y, -y3.x);  // times -i
-            xs[0] = make_double2(y0.x + y2.x, y0.y + y2.y);
-            xs[2 * h] = make_double2(y0.x - y2.x, y0.y - y2.y);
-            xs[h] = make_double2(y1.x + y3.x, y1.y + y3.y);
-            xs[3 * h] = make_double2(y1.x - y3.x, y1.y - y3.y);
+            const double2 a0 = make_double2(x0.x + t1.x, x0.y + t1.y), a1 = make_double2(x0.x - t1.x, x0.y - t1.y);
+            const double2 b0 = make_double2(t2.x + t3.x, t2.y + t3.y);
+            const double2 b1 = make_double2(t2.y - t3.y, t3.x - t2.x);  // -i (t2 - t3)
+            xs[0] = make_double2(a0.x + b0.x, a0.y + b0.y);
+            xs[2 * h] = make_double2(a0.x - b0.x, a0.y - b0.y);
+            xs[h] = make_double2(a1.x + b1.x, a1.y + b1.y);
+            xs[3 * h] = make_double2(a1.x - b1.x, a1.y - b1.y);
         }
     }
     if (h < N) {  // N = 2 h: the last radix-2 stage
