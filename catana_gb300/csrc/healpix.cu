@@ -82,18 +82,20 @@ __global__ void k_bin_gather(const double *pts, const uint32_t *perm, int64_t n,
 // argument k r is tested against the table's range [0, zmax) (a domain error otherwise);
 // unchecked launches are made only when the host has shown that the whole level lies in
 // range (0 <= r_min and k_max r_max < zmax, the same FP64 product as here), and form the
-// table position as r (k / dx) -- one rounding away from (k r) / dx, a change of the
-// interpolated value far below 1e-10 of the table's scale.
+// table position as r (k / dx) with kd[n] = k_ln / dx from the host -- one rounding away
+// from (k r) / dx, a change of the interpolated value far below 1e-10 of the table's
+// scale.
 template <bool CHECKED>
 __global__ void k_hp_map(const int64_t *__restrict__ offs, const double *__restrict__ r, int64_t npix, int nmax,
-                         const double *__restrict__ kln, const double *__restrict__ tab, int npts_tab, double dx_inv,
-                         double zmax, int l, double *__restrict__ map, int *err) {
+                         const double *__restrict__ kln, const double *__restrict__ kdl,
+                         const double *__restrict__ tab, int npts_tab, double dx_inv, double zmax, int l,
+                         double *__restrict__ map, int *err) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= npix * nmax) return;
     const int64_t pix = t / nmax;
     const int n = (int)(t - pix * nmax);
     const double k = kln[n];
-    const double kd = k * dx_inv;
+    const double kd = CHECKED ? 0.0 : kdl[n];
     double s = 0.0;
     for (int64_t q = offs[pix]; q < offs[pix + 1]; ++q) {
         double j;
@@ -645,10 +647,19 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
     const size_t mapb = al((size_t)npix * nmax * sizeof(double));
     const size_t ylmb = al((size_t)nrings * lmax * sizeof(double2));
     const size_t partb = al((size_t)nrings * lmax * nmax * sizeof(double2));
-    CG_CUDA_TRY(ctx->partial.ensure(mapb + ylmb + partb));
+    const size_t kdb = al((size_t)lmax * nmax * sizeof(double));
+    CG_CUDA_TRY(ctx->partial.ensure(mapb + ylmb + partb + kdb));
     double *map = ctx->partial.as<double>();
     double2 *ylm = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb);
     double2 *partial = reinterpret_cast<double2 *>(ctx->partial.as<char>() + mapb + ylmb);
+    double *kd_dev = reinterpret_cast<double *>(ctx->partial.as<char>() + mapb + ylmb + partb);
+    if (interpolated && kln_host) {  // k_ln / dx per (l, n): the unchecked map levels' table scale
+        std::vector<double> kd((size_t)lmax * nmax);
+        for (int l = 0; l < lmax; ++l)
+            for (int n = 0; n < nmax; ++n) kd[(size_t)l * nmax + n] = kln_host[(size_t)l * nmax + n] * ctx->tab_dxinv[l];
+        CG_CUDA_TRY(cudaMemcpyAsync(kd_dev, kd.data(), kd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
     const int npts_tab = 1000 * nmax;
     const size_t smem = (2 * HP_MAXPIX + 4 * HP_JC * HP_NB) * sizeof(double);
     const size_t smem_fft = (size_t)HF_G * R.max_pow2 * sizeof(double2);
@@ -665,7 +676,7 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
                               kln_host[(size_t)l * nmax + nmax - 1] * r_max < ctx->tab_zmax[l];
         auto map_kern = in_range ? k_hp_map<false> : k_hp_map<true>;
         map_kern<<<ceil_div(npix * nmax, 256), 256, 0, st>>>(
-            offsets_dev, r_sorted_dev, npix, nmax, kln_dev + (size_t)l * nmax,
+            offsets_dev, r_sorted_dev, npix, nmax, kln_dev + (size_t)l * nmax, kd_dev + (size_t)l * nmax,
             interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr, npts_tab,
             interpolated ? ctx->tab_dxinv[l] : 0.0, interpolated ? ctx->tab_zmax[l] : 0.0, l, map, err_dev);
         k_hp_ylm<<<ceil_div(nrings * (l + 1), 128), 128, 0, st>>>(ring_x, ring_phi, nrings, l, ctx->coef.as<double2>(),
