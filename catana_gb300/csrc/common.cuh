@@ -61,7 +61,7 @@ struct DeviceContext {
     int sm_count = 0;
     int cc_major = 0, cc_minor = 0;
     // workspace
-    DevBuf soa;        // point SoA (r, x, phi, w) of the current chunk
+    DevBuf soa;        // point SoA (r, x, w, cos phi, sin phi, phase fraction) of the current chunk
     DevBuf state;      // Legendre recurrence rows
     DevBuf partial;    // per-slab partial sums
     DevBuf flmn;       // f_lmn accumulator (complex, packed)

@@ -9,7 +9,8 @@
 //   * the Legendre values advance by one step of the l-recurrence from two stored
 //     rows P_{l-1}^m, P_{l-2}^m (FP64 [m][point] arrays in HBM), so each P_lm costs
 //     O(1) instead of O(l-m);
-//   * e^{-im phi} comes from one sincos per thread and m-run plus complex rotation;
+//   * e^{-im phi} comes from one sincospi of the exactly reduced phase frac(m u) per
+//     thread and m-run plus complex rotation by e^{i phi} (prepared once per point);
 //   * j_l comes from the reference's own linear table (1000*nmax nodes up to
 //     z_{l,nmax}, same node placement, same dx_inv, same lerp) or, in exact mode,
 //     from the direct evaluation in special.cuh;
@@ -20,6 +21,7 @@
 //     f_lmn accumulator (deterministic, no atomics).
 // The FP64 pipe bounds this path: 2*nmax*(l+1) FMAs per point per l.
 #include <cuda_runtime.h>
+#include <type_traits>
 #include <stdint.h>
 
 #include <algorithm>
@@ -38,16 +40,27 @@ namespace {
 constexpr int kTP = 32;        // points per shared-memory step
 constexpr int kThreads = 256;  // threads per CTA
 
-// AoS (r, theta, phi) -> SoA r, x = cos(theta), phi, w.
+// AoS (r, theta, phi) -> SoA r, x = cos(theta), w, (cos, sin)(phi) and the phase
+// fraction u = frac(phi / 2 pi) 2^64, from which e^{-i m phi} of any m follows exactly
+// (frac(m u) is exact in 64-bit arithmetic).
 __global__ void k_prep_points(const double *__restrict__ pts, const double *__restrict__ w, int64_t n,
-                              double *__restrict__ r_o, double *__restrict__ x_o, double *__restrict__ ph_o,
-                              double *__restrict__ w_o) {
+                              double *__restrict__ r_o, double *__restrict__ x_o, double *__restrict__ w_o,
+                              double *__restrict__ c1_o, double *__restrict__ s1_o,
+                              unsigned long long *__restrict__ u_o) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     r_o[i] = pts[3 * i];
     x_o[i] = cos(pts[3 * i + 1]);
-    ph_o[i] = pts[3 * i + 2];
     w_o[i] = w ? w[i] : 1.0;
+    const double ph = pts[3 * i + 2];
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    c1_o[i] = cs;
+    s1_o[i] = sn;
+    double f = ph * 0.15915494309189533576888376337251436;  // 1 / (2 pi)
+    f -= floor(f);
+    if (!(f < 1.0) || !(f >= 0.0)) f = 0.0;  // rounding up to 1, or a non-finite angle
+    u_o[i] = (unsigned long long)ldexp(f, 64);
 }
 
 // y[l][i] = j_l(0 + i*dx_l): FunctionInterpolator.cpp:12-19 with the node formula
@@ -63,7 +76,8 @@ __global__ void k_lerp_tables(double *__restrict__ tab, const double *__restrict
 struct LArgs {
     int l, nmax, nslabs;
     int64_t n;  // points in the chunk
-    const double *r, *x, *ph, *w;
+    const double *r, *x, *w, *c1, *s1;
+    const unsigned long long *u;  // phase fractions frac(phi / 2 pi) 2^64
     const double *kln;  // k_ln row of l (nmax)
     const double *tab;  // lerp table of l, or null for exact j_l
     int npts_tab;
@@ -96,6 +110,13 @@ __global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
     const int q = tid % kTP, g = tid / kTP;   // generator: point q, group g
     const int tx = tid % 16, ty = tid / 16;   // contraction: n = tx+16b, m = ty+16a
     const bool write_state = (blockIdx.z == 0);
+    // row sets u whose m = ty + 16 u lie past the block's count for the whole warp (its
+    // ty are 2w, 2w+1) skip the contraction: the test is warp-uniform
+    const int ty_warp = 2 * (tid / 32);
+    int urows = 0;
+#pragma unroll
+    for (int u = 0; u < TT; ++u)
+        if (ty_warp + 16 * u < mcount) urows = u + 1;
 
     double accR[TT][TT], accI[TT][TT];
 #pragma unroll
@@ -108,12 +129,15 @@ __global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
     for (int64_t base = i0; base < i1; base += kTP) {
         const int64_t i = base + q;
         const bool valid = i < i1;
-        double r = 0.0, x = 0.0, ph = 0.0, wi = 0.0;
+        double r = 0.0, x = 0.0, wi = 0.0, c1 = 1.0, s1 = 0.0;
+        unsigned long long uph = 0;
         if (valid) {
             r = a.r[i];
             x = a.x[i];
-            ph = a.ph[i];
             wi = a.w[i];
+            c1 = a.c1[i];
+            s1 = a.s1[i];
+            uph = a.u[i];
         }
         // ---- J[pt][n] = k_ln j_l(k_ln r) w ----
 #pragma unroll
@@ -145,17 +169,23 @@ __global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
         // ---- Y[pt][m] = P_lm(x) e^{-i m phi}, P by one recurrence step ----
         {
             const int ml0 = g * PER_G;
+            // e^{-i m phi} of the run's first m: 2 pi frac(m u) reduced exactly, as a
+            // fraction in [-1/2, 1/2) of a turn
+            const unsigned long long tm = (unsigned long long)(m0 + ml0) * uph;
             double sn, cs;
-            sincos((double)(m0 + ml0) * ph, &sn, &cs);
-            double er = cs, ei = -sn;  // e^{-i m phi}
-            double s1, c1;
-            sincos(ph, &s1, &c1);
+            sincospi((double)(long long)tm * 1.0842021724855044340074528008699e-19, &sn, &cs);  // 2^-63
+            double er = cs, ei = -sn;
 #pragma unroll
             for (int k = 0; k < PER_G; ++k) {
                 const int ml = ml0 + k;
                 const int m = m0 + ml;
+                if (ml >= mcount) {  // past this level's m: zero rows, no phase to advance
+                    sYr[q * LD + ml] = 0.0;
+                    sYi[q * LD + ml] = 0.0;
+                    continue;
+                }
                 double P = 0.0;
-                if (valid && ml < mcount) {
+                if (valid) {
                     if (l == 0) {
                         P = inv_sqrt4pi;
                     } else {
@@ -180,24 +210,32 @@ __global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
             }
         }
         __syncthreads();
-        // ---- f(m, n) += J(n) Y(m) ----
+        // ---- f(m, n) += J(n) Y(m), over the warp's live row sets only ----
+        auto contract = [&](auto rows_c) {
+            constexpr int U = decltype(rows_c)::value;
 #pragma unroll 4
-        for (int pp = 0; pp < kTP; ++pp) {
-            double jv[TT], yr[TT], yi[TT];
+            for (int pp = 0; pp < kTP; ++pp) {
+                double jv[TT], yr[U > 0 ? U : 1], yi[U > 0 ? U : 1];
 #pragma unroll
-            for (int u = 0; u < TT; ++u) {
-                yr[u] = sYr[pp * LD + ty + 16 * u];
-                yi[u] = sYi[pp * LD + ty + 16 * u];
-                jv[u] = sJ[pp * LD + tx + 16 * u];
-            }
-#pragma unroll
-            for (int u = 0; u < TT; ++u)
-#pragma unroll
-                for (int v = 0; v < TT; ++v) {
-                    accR[u][v] = fma(jv[v], yr[u], accR[u][v]);
-                    accI[u][v] = fma(jv[v], yi[u], accI[u][v]);
+                for (int u = 0; u < U; ++u) {
+                    yr[u] = sYr[pp * LD + ty + 16 * u];
+                    yi[u] = sYi[pp * LD + ty + 16 * u];
                 }
-        }
+#pragma unroll
+                for (int v = 0; v < TT; ++v) jv[v] = sJ[pp * LD + tx + 16 * v];
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int v = 0; v < TT; ++v) {
+                        accR[u][v] = fma(jv[v], yr[u], accR[u][v]);
+                        accI[u][v] = fma(jv[v], yi[u], accI[u][v]);
+                    }
+            }
+        };
+        if (urows == TT) contract(std::integral_constant<int, TT>());
+        else if (urows == 1) contract(std::integral_constant<int, 1>());
+        else if (TT == 4 && urows == 2) contract(std::integral_constant<int, (TT == 4 ? 2 : 1)>());
+        else if (TT == 4 && urows == 3) contract(std::integral_constant<int, (TT == 4 ? 3 : 1)>());
         __syncthreads();
     }
 #pragma unroll
@@ -315,7 +353,7 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
     // Chunk so that the three Legendre rows stay under ~1.5 GB.
     int64_t chunk = (int64_t)(1.5e9 / (3.0 * 8.0 * std::max(lmax, 1)));
     chunk = std::max<int64_t>(1024, std::min<int64_t>(chunk, npoints));
-    CG_CUDA_TRY(ctx->soa.ensure((size_t)chunk * 4 * sizeof(double)));
+    CG_CUDA_TRY(ctx->soa.ensure((size_t)chunk * 6 * sizeof(double)));
     CG_CUDA_TRY(ctx->state.ensure((size_t)chunk * 3 * std::max(lmax, 1) * sizeof(double)));
     double *soa = ctx->soa.as<double>();
     double *rows[3];
@@ -342,9 +380,10 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
 
     for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
         const int64_t nc = std::min(chunk, npoints - c0);
-        double *r = soa, *x = soa + chunk, *ph = soa + 2 * chunk, *w = soa + 3 * chunk;
+        double *r = soa, *x = soa + chunk, *w = soa + 2 * chunk, *c1 = soa + 3 * chunk, *s1 = soa + 4 * chunk;
+        unsigned long long *uph = reinterpret_cast<unsigned long long *>(soa + 5 * chunk);
         k_prep_points<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, weights_dev ? weights_dev + c0 : nullptr,
-                                                         nc, r, x, ph, w);
+                                                         nc, r, x, w, c1, s1, uph);
         count_launch();
         double *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
         for (int l = 0; l < lmax; ++l) {
@@ -361,8 +400,10 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
             a.n = nc;
             a.r = r;
             a.x = x;
-            a.ph = ph;
             a.w = w;
+            a.c1 = c1;
+            a.s1 = s1;
+            a.u = uph;
             a.kln = kln_dev + (size_t)l * nmax;
             a.tab = interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr;
             a.npts_tab = npts_tab;
@@ -486,7 +527,7 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
     const size_t b_tab = interpolated ? al(((size_t)lmax * npts_tab + lmax) * sizeof(double)) : 0;
     const size_t b_part = al((size_t)kNoAllocMaxSlabs * lmax * nmax * sizeof(double2));
     const size_t fixed = b_words + b_coef + b_tab + b_part;
-    const size_t per_point = (4 + 3 * (size_t)std::max<int>(lmax, 1)) * sizeof(double);
+    const size_t per_point = (6 + 3 * (size_t)std::max<int>(lmax, 1)) * sizeof(double);
     const int64_t min_chunk = std::min<int64_t>(std::max<int64_t>(npoints, 1), 1024);
     if (fixed + (size_t)min_chunk * per_point + 256 > kNoAllocBytes) {
         set_error("sfb_raw_noalloc: lmax=" + std::to_string(lmax) + ", nmax=" + std::to_string(nmax) +
@@ -521,7 +562,7 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
     int64_t chunk = (int64_t)(var_bytes / per_point);
     chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(npoints, 1)));
     double *soa = reinterpret_cast<double *>(var);
-    double *rows0 = soa + 4 * chunk;
+    double *rows0 = soa + 6 * chunk;
 
     CG_CUDA_TRY(cudaMemsetAsync(err_d, 0, sizeof(int), st));
     // k_ln on the host (cached zeros of the reference's zero finder)
@@ -572,9 +613,10 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
     for (int k = 0; k < 3; ++k) rows[k] = rows0 + (size_t)k * chunk * std::max<int>(lmax, 1);
     for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
         const int64_t nc = std::min(chunk, npoints - c0);
-        double *r = soa, *x = soa + chunk, *ph = soa + 2 * chunk, *w = soa + 3 * chunk;
+        double *r = soa, *x = soa + chunk, *w = soa + 2 * chunk, *c1 = soa + 3 * chunk, *s1 = soa + 4 * chunk;
+        unsigned long long *uph = reinterpret_cast<unsigned long long *>(soa + 5 * chunk);
         k_prep_points<<<ceil_div(nc, 256), 256, 0, st>>>(points_dev + 3 * c0, weights_dev ? weights_dev + c0 : nullptr,
-                                                         nc, r, x, ph, w);
+                                                         nc, r, x, w, c1, s1, uph);
         count_launch();
         double *st0 = rows[0], *st1 = rows[1], *st2 = rows[2];
         for (int l = 0; l < lmax; ++l) {
@@ -590,8 +632,10 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
             a.n = nc;
             a.r = r;
             a.x = x;
-            a.ph = ph;
             a.w = w;
+            a.c1 = c1;
+            a.s1 = s1;
+            a.u = uph;
             a.tab = interpolated ? tab_d + (size_t)l * npts_tab : nullptr;
             a.npts_tab = npts_tab;
             a.dx_inv = interpolated ? dxinv[l] : 0.0;
