@@ -26,14 +26,17 @@
 //     dominated by the FP32 coefficients), the argument formed as a float-float
 //     product so its absolute error is ~1e-12;
 //   * P_lm by one step of the l-recurrence from FP32 rows P_{l-1}, P_{l-2} in HBM
-//     (staged into shared memory one tile ahead with cp.async), with the recurrence
+//     (staged into shared memory one tile ahead by TMA), with the recurrence
 //     coefficients and x = cos(theta), s = sin(theta) as float-float pairs; the rows
 //     are stored scaled by 2^100 so that sectoral seeds down to 2^-226 stay
 //     representable (enough for lmax <= 256);
 //   * e^{-i m phi}: one sincospif of the exact phase (64-bit fixed-point fraction of a
 //     turn) per warp-run of <= 8 m, then complex rotation by e^{i phi}.
-// Pipeline: two operand buffers and two row stages; the MMAs of tile t run while the
-// CTA generates tile t+1.  Every wait on an mbarrier is bounded (1 s); on timeout the
+// Pipeline: two operand buffers and two row stages.  Warps 0..15 generate the operands
+// of tile t+1 while the tensor core multiplies tile t; warps 16..19 (one per TMEM lane
+// quadrant) fold D_tile into D_acc, flush, and issue each tile's MMAs, so the fold no
+// longer sits between a CTA barrier and the next MMA.  Hand-offs are mbarriers: operands
+// written, MMAs complete, row stage read.  Every wait is bounded (1 s); on timeout the
 // kernel records CATANA_ERR_CUDA in the error word, stops issuing work and frees its
 // tensor memory.
 #include <cuda.h>
@@ -57,7 +60,9 @@ namespace catana_gpu {
 namespace {
 
 constexpr int KT = 32;              // points per tile (two K=16 MMA steps)
-constexpr int NTHR = 512;           // 16 warps
+constexpr int NTHR = 512;           // 16 operand warps
+constexpr int NFOLDW = 4;           // fold / MMA warps, one per TMEM lane quadrant
+constexpr int NTOT = NTHR + 32 * NFOLDW;
 constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
 constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
 constexpr int FLUSH_FOLDS = 32;     // folds into the TMEM sum before it goes to global memory
@@ -212,13 +217,33 @@ __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c
 // FULLJ: every item of the launch has 128 radial orders in its half (no kmax cut):
 // each warp evaluates 8 J rows; otherwise the items' live row pairs are spread over
 // the warps and the rest of J stays zero.
+// one arrival (release, CTA scope) on an mbarrier
+__device__ __forceinline__ void ws_arrive(uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc05::smem_u32(mbar)) : "memory");
+}
+// named barrier 1 of the four fold warps (128 threads); fold_vote is the same barrier
+// returning the AND of every fold thread's flag, so the fold warps always agree
+__device__ __forceinline__ void fold_bar() { asm volatile("barrier.sync.aligned 1, 128;" ::: "memory"); }
+__device__ __forceinline__ bool fold_vote(bool v) {
+    int r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbarrier.red.and.aligned.pred q, 1, 128, p;\nselp.s32 %0, 1, 0, q;\n}"
+        : "=r"(r)
+        : "r"((int)v)
+        : "memory");
+    return r != 0;
+}
+
 template <bool EXT, bool FULLJ>
-__global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
+__global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ uint64_t mbar[2];  // MMA completion per operand buffer
     __shared__ uint64_t sbar[2];  // TMA completion per stage
     __shared__ uint32_t tmem_base_sh;
+    __shared__ uint64_t fbar[2];   // operands of buffer b written (NTHR arrivals)
+    __shared__ uint64_t gfree[2];  // stage s read by every operand thread (NTHR arrivals)
+    __shared__ int abort_sh;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int l = a.l;
@@ -241,9 +266,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     float *s_inv = reinterpret_cast<float *>(sm + OFF_INV);
     float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
-    for (int t = tid; t < 2 * a.nint; t += NTHR) s_tab[t] = a.tab[t];
+    for (int t = tid; t < 2 * a.nint; t += NTOT) s_tab[t] = a.tab[t];
     // radial orders past this half's count get k = 0 and J scale 0: their J rows are zero
-    for (int t = tid; t < NHALF / 2; t += NTHR) {
+    for (int t = tid; t < NHALF / 2; t += NTOT) {
         const float4 ka = 2 * t < nmax ? kz_row[2 * t] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 kb = 2 * t + 1 < nmax ? kz_row[2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
         s_kzp[t] = make_float4(ka.x, kb.x, ka.y, kb.y);
@@ -252,7 +277,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         s_inv[2 * t] = ka.w;
         s_inv[2 * t + 1] = kb.w;
     }
-    for (int t = tid; t < (mcount + 1) / 2; t += NTHR) {
+    for (int t = tid; t < (mcount + 1) / 2; t += NTOT) {
         const float4 ca = a.coef[mb0 + 2 * t];
         const float4 cb = 2 * t + 1 < mcount ? a.coef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
         s_coef[2 * t] = make_float4(ca.x, cb.x, ca.y, cb.y);
@@ -263,13 +288,18 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         tc05::mbar_init(&mbar[1], 1);
         tc05::mbar_init(&sbar[0], 1);
         tc05::mbar_init(&sbar[1], 1);
+        tc05::mbar_init(&fbar[0], NTHR);
+        tc05::mbar_init(&fbar[1], NTHR);
+        tc05::mbar_init(&gfree[0], NTHR);
+        tc05::mbar_init(&gfree[1], NTHR);
+        abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // J rows of radial orders past this half's count (a kmax cut, or nmax < 128) are zero
     // for the whole item: zero both operand buffers' J now; warps whose 8 rows are all
     // past the count then skip J entirely
     if (!FULLJ && nmax < NHALF) {
-        for (int t = tid; t < (int)(2 * SM_J / 16); t += NTHR) {
+        for (int t = tid; t < (int)(2 * SM_J / 16); t += NTOT) {
             *reinterpret_cast<uint4 *>(sm + t * 16) = make_uint4(0u, 0u, 0u, 0u);            // buffer 0
             *reinterpret_cast<uint4 *>(sm + SM_BUF + t * 16) = make_uint4(0u, 0u, 0u, 0u);  // buffer 1
         }
@@ -363,12 +393,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         return true;
     };
 
-    // D_acc (+)= D_tile, every warp: lane quadrant warp%4, column groups warp/4, +4, ...
+    // D_acc (+)= D_tile, by the fold warps: each its lane quadrant (warp % 4), every column group
     auto fold = [&]() {
         tc05::fence_after();
-        const int qd = warp & 3, cq = warp >> 2;
+        const int qd = warp & 3;
         const uint32_t lane_off = (uint32_t)(qd * 32) << 16;
-        for (int gi = cq; gi < (ncols_pad >> 4); gi += 4) {
+        for (int gi = 0; gi < (ncols_pad >> 4); ++gi) {
             uint32_t vt[16], va[16];
             tc05::tmem_ld16(d_tile + lane_off + gi * 16, vt);
             if (!acc_fresh) tc05::tmem_ld16(d_acc + lane_off + gi * 16, va);
@@ -392,9 +422,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
     // partial[cta] (+)= D_acc / (2^s_ln 2^12) (lane n), then the next fold restarts D_acc
     auto flush = [&]() {
         tc05::fence_after();
-        const int qd = warp & 3, cq = warp >> 2;
+        const int qd = warp & 3;
         const int lane_n = qd * 32 + lane;
-        for (int gi = cq; gi < (ncols_pad >> 4); gi += 4) {
+        for (int gi = 0; gi < (ncols_pad >> 4); ++gi) {
             uint32_t v[16];
             tc05::tmem_ld16(d_acc + ((uint32_t)(qd * 32) << 16) + gi * 16, v);
             tc05::tmem_wait_ld();
@@ -425,311 +455,345 @@ __global__ void __launch_bounds__(NTHR, 1) k_split_l(SplitArgs a) {
         folds = 0;
     };
 
-    prefetch_rows(t0);
-    for (int64_t t = t0; t < t1 && ok; ++t) {
-        const int b = (int)((t - t0) & 1);
-        prefetch_rows(t + 1);
-        // operand buffer b is free once the MMAs of tile t-2 have completed, and tile t is
-        // staged; each thread waits for itself (a failed wait aborts at the barrier below)
-        int tok = (wait_buf(b) && wait_stage((int)(t & 1))) ? 1 : 0;
-        uint8_t *bufp = sm + b * SM_BUF;
-        uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
-        const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
-        const float *stg2 = stg1 + MBLK * KT;
-        const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
-            sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE + 2 * SM_STROW + SM_STPTS);
-        const unsigned long long *stge2 = stge1 + MBLK;
-        const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
-                                                                2 * SM_STROW + q * 48);
-        const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
-        // ---- J tile: n = 8 g .. 8 g + 7 ----
-        if constexpr (FULLJ) {
-            const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
-            const float2 w2 = make_float2(pt.w, pt.w);
-            const int n0 = 8 * g;
-            float2 v[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int n = n0 + 2 * k;
-                const float4 kk = s_kzp[n >> 1];
-                const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
-                // z = r k as float-float: p + e
-                const float2 p = __fmul2_rn(rh2, kx);
-                float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
-                e = __ffma2_rn(rh2, ky, e);
-                e = __ffma2_rn(rl2, kx, e);
-                const float2 fl = make_float2(rintf(p.x), rintf(p.y));
-                const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);  // in [-1/2, 1/2]
-                // radii are checked on the host against the table's extent; clamp regardless
-                const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
-                const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
-                const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
-                const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
-                float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
-                ja = fmaf(ja, uu.x, a1.x);
-                jb = fmaf(jb, uu.y, b1.x);
-                ja = fmaf(ja, uu.x, a0.w);
-                jb = fmaf(jb, uu.y, b0.w);
-                ja = fmaf(ja, uu.x, a0.z);
-                jb = fmaf(jb, uu.y, b0.z);
-                ja = fmaf(ja, uu.x, a0.y);
-                jb = fmaf(jb, uu.y, b0.y);
-                ja = fmaf(ja, uu.x, a0.x);
-                jb = fmaf(jb, uu.y, b0.x);
-                const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
-                v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
+    // roles: warps 0..15 write each tile's operands (J, Y) into the two operand buffers;
+    // warps 16..19 (one per TMEM lane quadrant) fold the previous tile's tensor-core sum,
+    // flush, and issue the tile's MMAs.  Hand-offs: fbar[b] operands of buffer b written,
+    // mbar[b] the MMAs reading buffer b complete, gfree[s] stage s read by every operand
+    // thread (it may be refilled).  Every wait is bounded; a failed one raises abort_sh.
+    volatile int *abort_v = &abort_sh;
+    if (warp < NTHR / 32) {
+        uint32_t gw0 = 0, gw1 = 0;  // gfree phases waited (thread 0)
+        prefetch_rows(t0);
+        for (int64_t t = t0; t < t1; ++t) {
+            if (*abort_v) {
+                ok = false;
+                break;
             }
-            store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
-        }
-        else {
-            // fewer radial orders (a kmax cut, nmax < 128): their ceil(nmax / 2) row pairs
-            // spread evenly over the 16 warps (the rows past the count stay zero)
-            const int npr = (nmax + 1) >> 1;
-            const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
-            const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
-            const float2 w2 = make_float2(pt.w, pt.w);
-            for (int jp = jp0; jp < jp1; ++jp) {
-                const int n = 2 * jp;
-                const float4 kk = s_kzp[jp];
-                const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
-                const float2 p = __fmul2_rn(rh2, kx);
-                float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
-                e = __ffma2_rn(rh2, ky, e);
-                e = __ffma2_rn(rl2, kx, e);
-                const float2 fl = make_float2(rintf(p.x), rintf(p.y));
-                const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);
-                const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
-                const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
-                const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
-                const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
-                float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
-                ja = fmaf(ja, uu.x, a1.x);
-                jb = fmaf(jb, uu.y, b1.x);
-                ja = fmaf(ja, uu.x, a0.w);
-                jb = fmaf(jb, uu.y, b0.w);
-                ja = fmaf(ja, uu.x, a0.z);
-                jb = fmaf(jb, uu.y, b0.z);
-                ja = fmaf(ja, uu.x, a0.y);
-                jb = fmaf(jb, uu.y, b0.y);
-                ja = fmaf(ja, uu.x, a0.x);
-                jb = fmaf(jb, uu.y, b0.x);
-                const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
-                const float2 v = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
-                __half2 hh = __float22half2_rn(v);
-                const float2 hf = __half22float2(hh);
-                __half2 ll = __float22half2_rn(__fadd2_rn(v, make_float2(-hf.x, -hf.y)));
-                const uint32_t off = tc05::mn_sw128_off(n, q, 2);
-                *reinterpret_cast<__half2 *>(jhi + off) = hh;
-                *reinterpret_cast<__half2 *>(jlo + off) = ll;
+            const int b = (int)((t - t0) & 1);
+            bool okp = true;
+            if (tid == 0 && t > t0 && t + 1 < t1) {  // stage (t+1)&1 last held tile t-1
+                uint32_t &gw = ((t + 1) & 1) ? gw1 : gw0;
+                okp = tc05::mbar_wait(&gfree[(t + 1) & 1], gw & 1, WAIT_NS);
+                ++gw;
             }
-        }
-        // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
-        if (mlo < mhi) {
-            const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
-            // e^{i m phi} for the pair (m, m+1), times the readout factor 2^-88 of the scaled
-            // rows (exact): seed m, one rotation by e^{i phi}; pairs then advance by
-            // e^{2 i phi}.  nsm holds -sin.
-            float cma, sma;
-            phase_seed(pt.u, mb0 + mlo, cma, sma);
-            cma *= Y_UNSCALE;
-            sma *= Y_UNSCALE;
-            float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
-            float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
-            float *rowp = st0 + (int64_t)(mb0 + mlo) * stride + i;  // P_l row of the pair's first m
-            const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
-            const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
-            const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
-#pragma unroll
-            for (int pp = 0; pp < 4; ++pp) {
-                const int ml = mlo + 2 * pp;  // even local m
-                if (ml < mhi) {
-                    float2 yr, yi;
-                    {
-                        const int m = mb0 + ml;
-                        float2 P;
-                        if (m + 1 <= l - 2 && ml + 1 < mcount) {
-                            // both m take the plain three-term step: packed arithmetic
-                            const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
-                            const float2 p1 = make_float2(stg1[ml * KT + q], stg1[(ml + 1) * KT + q]);
-                            float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
-                            unsigned ea = 0, eb = 0;  // extended range: exponents of P_{l-1} at m, m+1
-                            if (EXT) {
-                                ea = ebits(stge1[ml], q);
-                                eb = ebits(stge1[ml + 1], q);
-                                const unsigned fa = ebits(stge2[ml], q), fb = ebits(stge2[ml + 1], q);
-                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                if (fa != ea) p2.x = (fa == ea + 1) ? p2.x * 0x1p-64f * 0x1p-64f : 0.f;
-                                if (fb != eb) p2.y = (fb == eb + 1) ? p2.y * 0x1p-64f * 0x1p-64f : 0.f;
-                            }
-                            const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
-                            const float2 bb =
-                                __ffma2_rn(make_float2(cb.z, cb.w), p2, __fmul2_rn(make_float2(cb.x, cb.y), p2));
-                            const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
-                            P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
-                            if (EXT) {  // renormalise values that grew past 2^40 while e > 0
-                                if (ea > 0 && fabsf(P.x) > 0x1p40f) {
-                                    P.x = P.x * 0x1p-64f * 0x1p-64f;
-                                    --ea;
-                                }
-                                if (eb > 0 && fabsf(P.y) > 0x1p40f) {
-                                    P.y = P.y * 0x1p-64f * 0x1p-64f;
-                                    --eb;
-                                }
-                            }
-                            if (wrows) {
-                                rowp[0] = P.x;
-                                rowp[stride] = P.y;
-                            }
-                            if (EXT && wrows) {
-                                const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
-                                const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
-                                const unsigned b0 = __ballot_sync(0xffffffffu, eb & 1u);
-                                const unsigned b1 = __ballot_sync(0xffffffffu, (eb >> 1) & 1u);
-                                if (lane == 0) {
-                                    ex0[t * cat.epitch + m] = ((unsigned long long)a1 << 32) | a0;
-                                    ex0[t * cat.epitch + m + 1] = ((unsigned long long)b1 << 32) | b0;
-                                }
-                            }
-                            if (EXT) {  // values with e > 0 are below 2^-188: no contribution
-                                if (ea) P.x = 0.f;
-                                if (eb) P.y = 0.f;
-                            }
-                        } else {
-                            // sectoral (m = l), m = l - 1, or the block's last odd m
-                            const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
-                            float pv[2];
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                const int mlh = ml + h, mh = m + h;
-                                float Pq = 0.f;
-                                unsigned e = 0;
-                                if (mlh < mhi) {  // warp-uniform
-                                    if (l == 0) {
-                                        Pq = P00_SCALED;
-                                    } else {
-                                        const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
-                                        const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
-                                        const bool sect = (mh == l);
-                                        const float p1 = stg1[(sect ? mlh - 1 : mlh) * KT + q];  // sectoral: P_{l-1,l-1}
-                                        const float xa = sect ? sh : xh, xb = sect ? sl : xl;
-                                        float p2 = (mh <= l - 2) ? stg2[mlh * KT + q] : 0.f;
-                                        if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
-                                            const unsigned long long w1 = stge1[sect ? mlh - 1 : mlh];
-                                            e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
-                                            if (mh <= l - 2) {
-                                                const unsigned long long w2 = stge2[mlh];
-                                                const unsigned e2 = (unsigned)((w2 >> q) & 1ull) |
-                                                                    ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
-                                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                                if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
-                                            }
-                                        }
-                                        const float tt = fmaf(xa, p1, xb * p1);
-                                        const float bb = fmaf(B_lo, p2, B_hi * p2);
-                                        const float vv = fmaf(A_lo, tt, -bb);
-                                        Pq = fmaf(A_hi, tt, vv);
-                                        if (EXT) {
-                                            const float ap = fabsf(Pq);
-                                            if (sect) {
-                                                if (ap < 0x1p-40f) {
-                                                    if (e < 3) {
-                                                        Pq = Pq * 0x1p64f * 0x1p64f;
-                                                        ++e;
-                                                    } else {
-                                                        Pq = 0.f;  // below 2^-520: no contribution within lmax
-                                                    }
-                                                }
-                                            } else if (e > 0 && ap > 0x1p40f) {
-                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
-                                                --e;
-                                            }
-                                        }
-                                    }
-                                    if (wrows) rowp[h ? stride : 0] = Pq;
-                                    if (EXT && wrows) {
-                                        const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
-                                        const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
-                                        if (lane == 0) ex0[t * cat.epitch + mh] = ((unsigned long long)b1w << 32) | b0w;
-                                    }
-                                    if (EXT && e != 0) Pq = 0.f;  // below 2^-188: no contribution
-                                }
-                                pv[h] = Pq;
-                            }
-                            P = make_float2(pv[0], pv[1]);
-                        }
-                        yr = __fmul2_rn(P, cm);
-                        yi = __fmul2_rn(P, nsm);
-                        // e^{i (m+2) phi} = e^{i m phi} e^{2 i phi}
-                        const float2 cmn = __ffma2_rn(cm, c22, __fmul2_rn(nsm, s22));
-                        nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
-                        cm = cmn;
-                    }
-                    store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
+            if (!okp) {
+                *abort_v = 1;
+                ok = false;
+                break;
+            }
+            prefetch_rows(t + 1);
+            if (!(wait_buf(b) && wait_stage((int)(t & 1)))) {
+                *abort_v = 1;
+                ok = false;
+                break;
+            }
+            uint8_t *bufp = sm + b * SM_BUF;
+            uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
+            const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
+            const float *stg2 = stg1 + MBLK * KT;
+            const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
+                sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE + 2 * SM_STROW + SM_STPTS);
+            const unsigned long long *stge2 = stge1 + MBLK;
+            const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                                                                    2 * SM_STROW + q * 48);
+            const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
+            // ---- J tile: n = 8 g .. 8 g + 7 ----
+            if constexpr (FULLJ) {
+                const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
+                const float2 w2 = make_float2(pt.w, pt.w);
+                const int n0 = 8 * g;
+                float2 v[4];
+    #pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int n = n0 + 2 * k;
+                    const float4 kk = s_kzp[n >> 1];
+                    const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
+                    // z = r k as float-float: p + e
+                    const float2 p = __fmul2_rn(rh2, kx);
+                    float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
+                    e = __ffma2_rn(rh2, ky, e);
+                    e = __ffma2_rn(rl2, kx, e);
+                    const float2 fl = make_float2(rintf(p.x), rintf(p.y));
+                    const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);  // in [-1/2, 1/2]
+                    // radii are checked on the host against the table's extent; clamp regardless
+                    const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
+                    const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
+                    const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                    const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
+                    float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
+                    ja = fmaf(ja, uu.x, a1.x);
+                    jb = fmaf(jb, uu.y, b1.x);
+                    ja = fmaf(ja, uu.x, a0.w);
+                    jb = fmaf(jb, uu.y, b0.w);
+                    ja = fmaf(ja, uu.x, a0.z);
+                    jb = fmaf(jb, uu.y, b0.z);
+                    ja = fmaf(ja, uu.x, a0.y);
+                    jb = fmaf(jb, uu.y, b0.y);
+                    ja = fmaf(ja, uu.x, a0.x);
+                    jb = fmaf(jb, uu.y, b0.x);
+                    const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
+                    v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
                 }
-                rowp += 2 * (int64_t)stride;
+                store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
             }
+            else {
+                // fewer radial orders (a kmax cut, nmax < 128): their ceil(nmax / 2) row pairs
+                // spread evenly over the 16 warps (the rows past the count stay zero)
+                const int npr = (nmax + 1) >> 1;
+                const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
+                const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
+                const float2 w2 = make_float2(pt.w, pt.w);
+                for (int jp = jp0; jp < jp1; ++jp) {
+                    const int n = 2 * jp;
+                    const float4 kk = s_kzp[jp];
+                    const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
+                    const float2 p = __fmul2_rn(rh2, kx);
+                    float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
+                    e = __ffma2_rn(rh2, ky, e);
+                    e = __ffma2_rn(rl2, kx, e);
+                    const float2 fl = make_float2(rintf(p.x), rintf(p.y));
+                    const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);
+                    const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
+                    const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
+                    const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                    const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
+                    float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
+                    ja = fmaf(ja, uu.x, a1.x);
+                    jb = fmaf(jb, uu.y, b1.x);
+                    ja = fmaf(ja, uu.x, a0.w);
+                    jb = fmaf(jb, uu.y, b0.w);
+                    ja = fmaf(ja, uu.x, a0.z);
+                    jb = fmaf(jb, uu.y, b0.z);
+                    ja = fmaf(ja, uu.x, a0.y);
+                    jb = fmaf(jb, uu.y, b0.y);
+                    ja = fmaf(ja, uu.x, a0.x);
+                    jb = fmaf(jb, uu.y, b0.x);
+                    const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
+                    const float2 v = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
+                    __half2 hh = __float22half2_rn(v);
+                    const float2 hf = __half22float2(hh);
+                    __half2 ll = __float22half2_rn(__fadd2_rn(v, make_float2(-hf.x, -hf.y)));
+                    const uint32_t off = tc05::mn_sw128_off(n, q, 2);
+                    *reinterpret_cast<__half2 *>(jhi + off) = hh;
+                    *reinterpret_cast<__half2 *>(jlo + off) = ll;
+                }
+            }
+            // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
+            if (mlo < mhi) {
+                const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
+                // e^{i m phi} for the pair (m, m+1), times the readout factor 2^-88 of the scaled
+                // rows (exact): seed m, one rotation by e^{i phi}; pairs then advance by
+                // e^{2 i phi}.  nsm holds -sin.
+                float cma, sma;
+                phase_seed(pt.u, mb0 + mlo, cma, sma);
+                cma *= Y_UNSCALE;
+                sma *= Y_UNSCALE;
+                float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
+                float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
+                float *rowp = st0 + (int64_t)(mb0 + mlo) * stride + i;  // P_l row of the pair's first m
+                const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
+                const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
+                const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
+    #pragma unroll
+                for (int pp = 0; pp < 4; ++pp) {
+                    const int ml = mlo + 2 * pp;  // even local m
+                    if (ml < mhi) {
+                        float2 yr, yi;
+                        {
+                            const int m = mb0 + ml;
+                            float2 P;
+                            if (m + 1 <= l - 2 && ml + 1 < mcount) {
+                                // both m take the plain three-term step: packed arithmetic
+                                const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
+                                const float2 p1 = make_float2(stg1[ml * KT + q], stg1[(ml + 1) * KT + q]);
+                                float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
+                                unsigned ea = 0, eb = 0;  // extended range: exponents of P_{l-1} at m, m+1
+                                if (EXT) {
+                                    ea = ebits(stge1[ml], q);
+                                    eb = ebits(stge1[ml + 1], q);
+                                    const unsigned fa = ebits(stge2[ml], q), fb = ebits(stge2[ml + 1], q);
+                                    // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                    if (fa != ea) p2.x = (fa == ea + 1) ? p2.x * 0x1p-64f * 0x1p-64f : 0.f;
+                                    if (fb != eb) p2.y = (fb == eb + 1) ? p2.y * 0x1p-64f * 0x1p-64f : 0.f;
+                                }
+                                const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
+                                const float2 bb =
+                                    __ffma2_rn(make_float2(cb.z, cb.w), p2, __fmul2_rn(make_float2(cb.x, cb.y), p2));
+                                const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
+                                P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                                if (EXT) {  // renormalise values that grew past 2^40 while e > 0
+                                    if (ea > 0 && fabsf(P.x) > 0x1p40f) {
+                                        P.x = P.x * 0x1p-64f * 0x1p-64f;
+                                        --ea;
+                                    }
+                                    if (eb > 0 && fabsf(P.y) > 0x1p40f) {
+                                        P.y = P.y * 0x1p-64f * 0x1p-64f;
+                                        --eb;
+                                    }
+                                }
+                                if (wrows) {
+                                    rowp[0] = P.x;
+                                    rowp[stride] = P.y;
+                                }
+                                if (EXT && wrows) {
+                                    const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
+                                    const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
+                                    const unsigned b0 = __ballot_sync(0xffffffffu, eb & 1u);
+                                    const unsigned b1 = __ballot_sync(0xffffffffu, (eb >> 1) & 1u);
+                                    if (lane == 0) {
+                                        ex0[t * cat.epitch + m] = ((unsigned long long)a1 << 32) | a0;
+                                        ex0[t * cat.epitch + m + 1] = ((unsigned long long)b1 << 32) | b0;
+                                    }
+                                }
+                                if (EXT) {  // values with e > 0 are below 2^-188: no contribution
+                                    if (ea) P.x = 0.f;
+                                    if (eb) P.y = 0.f;
+                                }
+                            } else {
+                                // sectoral (m = l), m = l - 1, or the block's last odd m
+                                const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
+                                float pv[2];
+    #pragma unroll
+                                for (int h = 0; h < 2; ++h) {
+                                    const int mlh = ml + h, mh = m + h;
+                                    float Pq = 0.f;
+                                    unsigned e = 0;
+                                    if (mlh < mhi) {  // warp-uniform
+                                        if (l == 0) {
+                                            Pq = P00_SCALED;
+                                        } else {
+                                            const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
+                                            const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
+                                            const bool sect = (mh == l);
+                                            const float p1 = stg1[(sect ? mlh - 1 : mlh) * KT + q];  // sectoral: P_{l-1,l-1}
+                                            const float xa = sect ? sh : xh, xb = sect ? sl : xl;
+                                            float p2 = (mh <= l - 2) ? stg2[mlh * KT + q] : 0.f;
+                                            if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
+                                                const unsigned long long w1 = stge1[sect ? mlh - 1 : mlh];
+                                                e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
+                                                if (mh <= l - 2) {
+                                                    const unsigned long long w2 = stge2[mlh];
+                                                    const unsigned e2 = (unsigned)((w2 >> q) & 1ull) |
+                                                                        ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
+                                                    // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                                    if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
+                                                }
+                                            }
+                                            const float tt = fmaf(xa, p1, xb * p1);
+                                            const float bb = fmaf(B_lo, p2, B_hi * p2);
+                                            const float vv = fmaf(A_lo, tt, -bb);
+                                            Pq = fmaf(A_hi, tt, vv);
+                                            if (EXT) {
+                                                const float ap = fabsf(Pq);
+                                                if (sect) {
+                                                    if (ap < 0x1p-40f) {
+                                                        if (e < 3) {
+                                                            Pq = Pq * 0x1p64f * 0x1p64f;
+                                                            ++e;
+                                                        } else {
+                                                            Pq = 0.f;  // below 2^-520: no contribution within lmax
+                                                        }
+                                                    }
+                                                } else if (e > 0 && ap > 0x1p40f) {
+                                                    Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                    --e;
+                                                }
+                                            }
+                                        }
+                                        if (wrows) rowp[h ? stride : 0] = Pq;
+                                        if (EXT && wrows) {
+                                            const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
+                                            const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
+                                            if (lane == 0) ex0[t * cat.epitch + mh] = ((unsigned long long)b1w << 32) | b0w;
+                                        }
+                                        if (EXT && e != 0) Pq = 0.f;  // below 2^-188: no contribution
+                                    }
+                                    pv[h] = Pq;
+                                }
+                                P = make_float2(pv[0], pv[1]);
+                            }
+                            yr = __fmul2_rn(P, cm);
+                            yi = __fmul2_rn(P, nsm);
+                            // e^{i (m+2) phi} = e^{i m phi} e^{2 i phi}
+                            const float2 cmn = __ffma2_rn(cm, c22, __fmul2_rn(nsm, s22));
+                            nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
+                            cm = cmn;
+                        }
+                        store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
+                    }
+                    rowp += 2 * (int64_t)stride;
+                }
+            }
+            tc05::fence_proxy_async();
+            ws_arrive(&gfree[t & 1]);
+            ws_arrive(&fbar[b]);
+            if (b) ++uses1; else ++uses0;
         }
-        tc05::fence_proxy_async();
-        // ---- every FOLD_TILES tiles: fold the tensor-core sum into D_acc (needs its MMAs complete) ----
-        const bool fold_now = (t > t0) && ((t - t0) % FOLD_TILES == 0);
-        if (fold_now) {  // each warp folds (and flushes) its own TMEM columns
-            const int pb = b ^ 1;
-            if (__all_sync(0xffffffffu, wait_buf(pb))) {
+        // stage loads still in flight (a loop that stopped early) land before the CTA exits
+        while (swait0 < sfill0 && wait_stage(0)) {
+        }
+        while (swait1 < sfill1 && wait_stage(1)) {
+        }
+    } else {
+        uint32_t fw0 = 0, fw1 = 0;  // fbar phases waited
+        for (int64_t t = t0; t < t1; ++t) {
+            const int b = (int)((t - t0) & 1);
+            uint32_t &fw = b ? fw1 : fw0;
+            bool okw = tc05::mbar_wait(&fbar[b], fw & 1, WAIT_NS);
+            ++fw;
+            if (okw && t > t0) okw = wait_buf(b ^ 1);  // the MMAs of tile t-1 (D_tile) complete
+            if (!fold_vote(okw && !*abort_v)) {        // the fold warps decide together
+                *abort_v = 1;
+                ok = false;
+                break;
+            }
+            if (t > t0) {
                 fold();
                 if (folds == FLUSH_FOLDS) flush();
-            } else {
-                tok = 0;
+            }
+            tc05::fence_before();
+            fold_bar();
+            tc05::fence_after();
+            uint8_t *bufp = sm + b * SM_BUF;
+            uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
+            const bool fresh_tile = ((t - t0) % FOLD_TILES == 0);  // D_tile was folded (or never used)
+            if (tid == NTHR) {
+                const uint32_t sj_hi = tc05::smem_u32(jhi), sj_lo = tc05::smem_u32(jlo);
+                const uint32_t sy_hi = tc05::smem_u32(yhi), sy_lo = tc05::smem_u32(ylo);
+    #pragma unroll
+                for (int ks = 0; ks < 2; ++ks) {
+                    const uint64_t ah = tc05::desc_sw128(sj_hi + ks * 4096, 1024, 2048);
+                    const uint64_t al = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
+                    const uint64_t bh = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
+                    const uint64_t bl = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
+                    tc05::mma_f16(d_tile, ah, bh, idesc, (ks == 0 && fresh_tile) ? 0u : 1u);
+                    tc05::mma_f16(d_tile, ah, bl, idesc, 1u);
+                    tc05::mma_f16(d_tile, al, bh, idesc, 1u);
+                }
+                tc05::commit(&mbar[b]);
+            }
+            if (b) ++uses1; else ++uses0;
+        }
+        if (ok && t1 > t0) {
+            const int lb = (int)((t1 - 1 - t0) & 1);
+            ok = fold_vote(wait_buf(lb));
+            if (ok) {
+                fold();
+                flush();
             }
         }
-        tc05::fence_before();
-        if (!__syncthreads_and(tok)) {
-            ok = false;
-            break;
-        }
-        tc05::fence_after();
-        // ---- hand tile t to the tensor cores: D_tile (+)= Jhi Yhi + Jhi Ylo + Jlo Yhi ----
-        const bool fresh_tile = ((t - t0) % FOLD_TILES == 0);  // D_tile was folded (or never used)
-        if (tid == 0) {
-            const uint32_t sj_hi = tc05::smem_u32(jhi), sj_lo = tc05::smem_u32(jlo);
-            const uint32_t sy_hi = tc05::smem_u32(yhi), sy_lo = tc05::smem_u32(ylo);
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks) {
-                const uint64_t ah = tc05::desc_sw128(sj_hi + ks * 4096, 1024, 2048);
-                const uint64_t al = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
-                const uint64_t bh = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
-                const uint64_t bl = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
-                tc05::mma_f16(d_tile, ah, bh, idesc, (ks == 0 && fresh_tile) ? 0u : 1u);
-                tc05::mma_f16(d_tile, ah, bl, idesc, 1u);
-                tc05::mma_f16(d_tile, al, bh, idesc, 1u);
-            }
-            tc05::commit(&mbar[b]);
-        }
-        if (b) ++uses1; else ++uses0;
-    }
-    // last tile: fold and flush
-    if (ok && t1 > t0) {
-        const int lb = (int)((t1 - 1 - t0) & 1);
-        ok = __syncthreads_and(wait_buf(lb) ? 1 : 0) != 0;
-        if (ok) {
-            fold();
-            flush();
+        if (ok) ok = fold_vote(wait_buf(0) && wait_buf(1));
+        if (!ok) {
+            // give in-flight MMAs a last bounded chance to land before TMEM is released
+            wait_buf(0);
+            wait_buf(1);
+            *abort_v = 1;
         }
     }
-    if (ok) ok = __syncthreads_and((wait_buf(0) && wait_buf(1)) ? 1 : 0) != 0;
-    if (!ok) {
-        // give in-flight MMAs a last bounded chance to land before TMEM is released
-        wait_buf(0);
-        wait_buf(1);
-        if (tid == 0) *a.err = CATANA_ERR_CUDA;
-    }
-    // stage loads still in flight (a loop that stopped early) land before the CTA exits
-    while (swait0 < sfill0 && wait_stage(0)) {
-    }
-    while (swait1 < sfill1 && wait_stage(1)) {
-    }
+    if (!ok && (tid == 0 || tid == NTHR)) *a.err = CATANA_ERR_CUDA;
     // an empty slab still owns partial rows: write zeros so the reduction sees them
     if (t0 >= t1) {
-        for (int t = tid; t < ncols * 128; t += NTHR) partial_cta[t] = 0.f;
+        for (int t = tid; t < ncols * 128; t += NTOT) partial_cta[t] = 0.f;
     }
     tc05::fence_before();
     __syncthreads();
@@ -1445,7 +1509,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                             if (l >= lmax_g) continue;
                             const int ni = S.item0[l + 1] - S.item0[l];
                             if (ni == 0) continue;
-                            kern_for(S.fullj[l] != 0)<<<ni, NTHR, SMEM_BYTES, st>>>(level_args(S, l));
+                            kern_for(S.fullj[l] != 0)<<<ni, NTOT, SMEM_BYTES, st>>>(level_args(S, l));
                             count_launch();
                         }
                         CG_CUDA_TRY(cudaGetLastError());
@@ -1476,7 +1540,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const int nr = S.red0[l + 1] - S.red0[l];
                 if (ni == 0) continue;
                 if (profile) prof_begin(ls_st);
-                kern_for(S.fullj[l] != 0)<<<ni, NTHR, SMEM_BYTES, ls_st>>>(level_args(S, l));
+                kern_for(S.fullj[l] != 0)<<<ni, NTOT, SMEM_BYTES, ls_st>>>(level_args(S, l));
                 if (profile) prof_end(ls_st, S.flops[l]);
                 dim3 rg(ceil_div((int64_t)(l + 1) * S.maxn[l], 128), nr);
                 k_split_reduce<<<rg, 128, 0, ls_st>>>(partial, l + 1,
