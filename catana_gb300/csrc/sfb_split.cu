@@ -65,7 +65,7 @@ constexpr int NFOLDW = 4;           // fold / MMA warps, one per TMEM lane quadr
 constexpr int NTOT = NTHR + 32 * NFOLDW;
 constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
 constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
-constexpr int FLUSH_FOLDS = 32;     // folds into the TMEM sum before it goes to global memory
+constexpr int FLUSH_FOLDS = 128;    // folds into the TMEM sum before it goes to global memory
 constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
 constexpr double H = 1.0;           // table interval width in z (intervals centred on integers)
 constexpr int TDEG = 6;             // table polynomial degree (7 coefficients in two float4)
@@ -680,9 +680,16 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                                 }
                                             }
                                             const float tt = fmaf(xa, p1, xb * p1);
-                                            const float bb = fmaf(B_lo, p2, B_hi * p2);
-                                            const float vv = fmaf(A_lo, tt, -bb);
-                                            Pq = fmaf(A_hi, tt, vv);
+                                            // B P_{l-2} as bh + bl with bh's rounding error kept in bl:
+                                            // at l = 2, m = 0 P_{l-2} = P_00 is the same for every
+                                            // point, and one rounded product would be one error
+                                            // shared by all points -- a monopole component in Y_20
+                                            // that the (coherent) monopole of the catalog leaks
+                                            // through, growing like sqrt(N) against the l = 2 signal
+                                            const float bh = B_hi * p2;
+                                            const float bl = fmaf(B_lo, p2, fmaf(B_hi, p2, -bh));
+                                            const float vv = fmaf(A_lo, tt, -bl);
+                                            Pq = fmaf(A_hi, tt, -bh) + vv;
                                             if (EXT) {
                                                 const float ap = fabsf(Pq);
                                                 if (sect) {

@@ -1,6 +1,6 @@
 """The split-precision tensor-core form (tcgen05, 3-term FP16 hi+lo products, FP32
-accumulation folded per 32-point tile, FP64 across tiles) against the FP64 oracle with
-exact j_l.
+accumulation folded per 32-point tile, FP32 partial per work item, FP64 across items)
+against the FP64 oracle with exact j_l.
 
 Error measures (measured values are ~2e-7 median, ~6e-7 p99 on 100k points):
   C_ln   median relative error <= 5e-7 and 99th percentile <= 2e-6; every entry
@@ -44,7 +44,7 @@ def _check(res, f, c, tag):
     (3000, 8, 8, False),
     (5000, 33, 20, True),
     (2000, 130, 64, False),   # l >= 128: two m-blocks per slab
-    (20000, 40, 100, False),  # many tiles per CTA: folds and flushes
+    (20000, 40, 100, False),  # several tiles per CTA: per-tile folds
     (3000, 24, 200, True),    # nmax > 128: two radial halves
 ])
 def test_split_vs_oracle(sm103, n, lmax, nmax, weighted):
@@ -68,6 +68,22 @@ def test_split_full_shape_vs_fp64_gpu(sm103):
     rs = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, precision="split")
     rp = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, interpolation="off")
     _check(rs, rp.f_lmn, rp.c_ln, "split lmax=256 nmax=128 n=20000")
+
+
+def test_split_long_items_vs_fp64_gpu(sm103):
+    """2M points: about 400 tiles per work item, so each item folds into its TMEM sum
+    and flushes it into its running FP32 partial several times (read-modify-write of
+    the partial) before the last flush; split vs the plain FP64 GPU path with exact j_l
+    on the same points.  At this size the catalog's monopole (a sum that grows like N)
+    leaks through any error of Y_lm with a component along Y_00; the l = 2, m = 0 step
+    keeps B P_00 unrounded for that reason."""
+    n = 2_000_000
+    pts = uniform_ball(n, 1000.0, seed=77)
+    w = np.random.default_rng(77).uniform(0.5, 1.5, n)
+    pc = catana.PointContainer(pts)
+    rs = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, precision="split")
+    rp = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, interpolation="off")
+    _check(rs, rp.f_lmn, rp.c_ln, "split lmax=64 nmax=32 n=2M")
 
 
 def test_split_multi_chunk_linearity(sm103):
