@@ -234,6 +234,34 @@ __device__ __forceinline__ bool fold_vote(bool v) {
     return r != 0;
 }
 
+// A tt - B p2 rounded once (A = ah + al, B = bh + bl as float-float): TwoSum of the two
+// large products, plus their exact remainders.  The usual fma chain rounds a partial sum
+// that the large B p2 dominates, so the small A_lo tt term is absorbed -- and it has a
+// nonzero mean over the sphere for m = 0, which puts a monopole component into Y_l0 that
+// a catalog's monopole (a sum growing like N) leaks through into l > 0.  Explicit _rn
+// operations keep the compiler from contracting or reassociating the TwoSum.
+__device__ __forceinline__ float step_once(float ah, float al, float bh, float bl, float tt, float p2) {
+    const float p_hi = __fmul_rn(ah, tt);
+    const float p_lo = fmaf(ah, tt, -p_hi);
+    const float q_hi = __fmul_rn(bh, p2);
+    const float q_lo = fmaf(bl, p2, fmaf(bh, p2, -q_hi));
+    const float s = __fadd_rn(p_hi, -q_hi);
+    const float v = __fadd_rn(s, -p_hi);
+    const float se = __fadd_rn(__fadd_rn(p_hi, -__fadd_rn(s, -v)), __fadd_rn(-q_hi, -v));
+    return __fadd_rn(s, __fadd_rn(se, __fadd_rn(p_lo, fmaf(al, tt, -q_lo))));
+}
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ float2 step_once2(float2 ah, float2 al, float2 bh, float2 bl, float2 tt, float2 p2) {
+    const float2 p_hi = __fmul2_rn(ah, tt);
+    const float2 p_lo = __ffma2_rn(ah, tt, neg2(p_hi));
+    const float2 q_hi = __fmul2_rn(bh, p2);
+    const float2 q_lo = __ffma2_rn(bl, p2, __ffma2_rn(bh, p2, neg2(q_hi)));
+    const float2 s = __fadd2_rn(p_hi, neg2(q_hi));
+    const float2 v = __fadd2_rn(s, neg2(p_hi));
+    const float2 se = __fadd2_rn(__fadd2_rn(p_hi, neg2(__fadd2_rn(s, neg2(v)))), __fadd2_rn(neg2(q_hi), neg2(v)));
+    return __fadd2_rn(s, __fadd2_rn(se, __fadd2_rn(p_lo, __ffma2_rn(al, tt, neg2(q_lo)))));
+}
+
 template <bool EXT, bool FULLJ>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     extern __shared__ uint8_t smem_raw[];
@@ -617,10 +645,16 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                     if (fb != eb) p2.y = (fb == eb + 1) ? p2.y * 0x1p-64f * 0x1p-64f : 0.f;
                                 }
                                 const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
-                                const float2 bb =
-                                    __ffma2_rn(make_float2(cb.z, cb.w), p2, __fmul2_rn(make_float2(cb.x, cb.y), p2));
-                                const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
-                                P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                                if (m == 0) {  // the m = 0 column rounded once (step_once)
+                                    P = step_once2(make_float2(ca.x, ca.y), make_float2(ca.z, ca.w),
+                                                   make_float2(cb.x, cb.y), make_float2(cb.z, cb.w), tt, p2);
+                                } else {
+                                    const float2 bb = __ffma2_rn(make_float2(cb.z, cb.w), p2,
+                                                                 __fmul2_rn(make_float2(cb.x, cb.y), p2));
+                                    const float2 vv =
+                                        __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
+                                    P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                                }
                                 if (EXT) {  // renormalise values that grew past 2^40 while e > 0
                                     if (ea > 0 && fabsf(P.x) > 0x1p40f) {
                                         P.x = P.x * 0x1p-64f * 0x1p-64f;
@@ -680,16 +714,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                                 }
                                             }
                                             const float tt = fmaf(xa, p1, xb * p1);
-                                            // B P_{l-2} as bh + bl with bh's rounding error kept in bl:
-                                            // at l = 2, m = 0 P_{l-2} = P_00 is the same for every
-                                            // point, and one rounded product would be one error
-                                            // shared by all points -- a monopole component in Y_20
-                                            // that the (coherent) monopole of the catalog leaks
-                                            // through, growing like sqrt(N) against the l = 2 signal
-                                            const float bh = B_hi * p2;
-                                            const float bl = fmaf(B_lo, p2, fmaf(B_hi, p2, -bh));
-                                            const float vv = fmaf(A_lo, tt, -bl);
-                                            Pq = fmaf(A_hi, tt, -bh) + vv;
+                                            // rounded once (step_once); at l = 2, m = 0 P_{l-2} = P_00
+                                            // is the same for every point, so the fma chain's error
+                                            // would even be one constant shared by all points
+                                            Pq = step_once(A_hi, A_lo, B_hi, B_lo, tt, p2);
                                             if (EXT) {
                                                 const float ap = fabsf(Pq);
                                                 if (sect) {
