@@ -75,8 +75,8 @@ def test_split_long_items_vs_fp64_gpu(sm103):
     and flushes it into its running FP32 partial several times (read-modify-write of
     the partial) before the last flush; split vs the plain FP64 GPU path with exact j_l
     on the same points.  At this size the catalog's monopole (a sum that grows like N)
-    leaks through any error of Y_lm with a component along Y_00; the l = 2, m = 0 step
-    keeps B P_00 unrounded for that reason."""
+    leaks through any error of Y_l0 with a nonzero mean over the sphere; the m = 0
+    Legendre steps round A x P_{l-1} - B P_{l-2} once for that reason."""
     n = 2_000_000
     pts = uniform_ball(n, 1000.0, seed=77)
     w = np.random.default_rng(77).uniform(0.5, 1.5, n)
