@@ -29,7 +29,9 @@
 //     (staged into shared memory one tile ahead by TMA), with the recurrence
 //     coefficients and x = cos(theta), s = sin(theta) as float-float pairs; the rows
 //     are stored scaled by 2^100 so that sectoral seeds down to 2^-226 stay
-//     representable (enough for lmax <= 256);
+//     representable (enough for lmax <= 256); the m = 0 step is rounded once
+//     (step_once), so Y_l0 carries no mean error over the sphere through which a
+//     catalog's monopole could leak into l > 0;
 //   * e^{-i m phi}: one sincospif of the exact phase (64-bit fixed-point fraction of a
 //     turn) per warp-run of <= 8 m, then complex rotation by e^{i phi}.
 // Pipeline: two operand buffers and two row stages.  Warps 0..15 generate the operands
