@@ -682,6 +682,27 @@ def main():
                                        "f_lmn_rms_err_over_rms_f_by_l": {"l=0": float(rms_l[0]),
                                                                          "l=%d" % (L // 2): float(rms_l[L // 2]),
                                                                          "l=%d" % (L - 1): float(rms_l[-1])}}
+            # ---- the same at many tiles per work item (folds, flushes, a catalog monopole
+            # growing like N): 2M points of the catalog at lmax 64, nmax 32 ----
+            try:
+                n2 = min(2_000_000, a.points)
+                pc2 = catana.PointContainer(np.ascontiguousarray(pts[:n2]))
+                w2 = np.ascontiguousarray(w[:n2])
+                rs2 = catana.sfb_decomposition(pc2, 64, 32, a.rmax, True, False, weights=w2, precision="split")
+                rp2 = catana.sfb_decomposition(pc2, 64, 32, a.rmax, True, False, weights=w2, interpolation="off")
+                rel2 = np.abs(rs2.c_ln - rp2.c_ln) / np.abs(rp2.c_ln)
+                typ2 = np.abs(rs2.c_ln - rp2.c_ln) / np.maximum(np.abs(rp2.c_ln),
+                                                                np.median(rp2.c_ln, axis=1, keepdims=True))
+                rms2 = max(np.sqrt(np.mean(np.abs(x - y) ** 2) / np.mean(np.abs(y) ** 2))
+                           for x, y in zip(rs2.f_lmn, rp2.f_lmn))
+                out["accuracy_vs_fp64_2M_l64_n32"] = {
+                    "sample_points": n2, "reference": "FP64 plain GPU path, exact j_l",
+                    "c_ln_rel_err_median": float(np.median(rel2)), "c_ln_rel_err_p99": float(np.percentile(rel2, 99)),
+                    "c_ln_rel_err_max": float(rel2.max()),
+                    "c_ln_abs_err_over_max_c_or_median_c_l_max": float(typ2.max()),
+                    "f_lmn_rms_err_over_rms_f_max_over_l": float(rms2)}
+            except Exception as ex:  # a side measurement: never costs the main line
+                out["accuracy_vs_fp64_2M_l64_n32"] = {"error": repr(ex)}
         # ---- side workloads: FP64 plain at 100k points / lmax = nmax = 32, HEALPix nside 256 ----
         if a.side:
             out["side"] = side_workloads(torch, _lib, catana, sp)
