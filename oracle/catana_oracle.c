@@ -500,6 +500,51 @@ int co_bin_points(int64_t nside, const double *pts, int64_t npoints, int64_t *of
 /* F[rpix - m%rpix] instead of its conjugate (sfb_reverse_fft.cpp:192-207).  */
 /* The DFT is evaluated directly for the frequencies the extraction reads.    */
 /* ------------------------------------------------------------------------- */
+/* One multipole's pixel maps for the FFT form of the HEALPix SFB (oracle.sfb_healpix_fft):
+ * map[pix * nmax + n] = sum over the pixel's points, in order, of j_l(k_ln r) -- the same
+ * sums as the map loop of co_sfb_healpix (sfb_reverse_fft.cpp:91-113), with the same j_l
+ * rule (the lerp table of SBesselInterpolator.cpp:10-26 or the direct j_l).  Returns 2 when
+ * an argument lies outside the table. */
+int co_healpix_maps(int64_t npix, const int64_t *offsets, const double *r_sorted, int l, int nmax,
+                    const double *k_row, double rmax, int interpolated, int nthreads, double *map)
+{
+    (void)rmax;
+    if (nthreads <= 0) {
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#else
+        nthreads = 1;
+#endif
+    }
+    int npts_tab = 1000 * nmax;
+    double *table = NULL, dx_inv = 0.0, zmax = 0.0;
+    if (interpolated) {
+        double *zl = (double *)malloc(sizeof(double) * (nmax + 1 > 2 ? nmax + 1 : 2));
+        co_sbessel_zeros((unsigned)l, nmax + 1, zl);
+        zmax = zl[nmax];
+        free(zl);
+        table = (double *)malloc(sizeof(double) * npts_tab);
+        co_lerp_table(l, zmax, npts_tab, table, &dx_inv);
+    }
+    int err_any = 0;
+#pragma omp parallel for num_threads(nthreads) schedule(static) reduction(| : err_any)
+    for (int64_t p = 0; p < npix; ++p) {
+        int err = 0;
+        for (int n = 0; n < nmax; ++n) {
+            const double k_n = k_row[n];
+            double s = 0.0;
+            for (int64_t q = offsets[p]; q < offsets[p + 1]; ++q) {
+                const double z = k_n * r_sorted[q];
+                s += interpolated ? co_lerp_eval(table, npts_tab, dx_inv, zmax, z, &err) : co_sbessel_jl(l, z);
+            }
+            map[p * nmax + n] = s;
+        }
+        err_any |= err;
+    }
+    free(table);
+    return err_any ? 2 : 0;
+}
+
 int co_sfb_healpix(int64_t nside, const int64_t *offsets, const double *r_sorted, int lmax, int nmax, double rmax,
                    int interpolated, int nthreads, double *k_ln, double *c_ln, double *f_re, double *f_im)
 {

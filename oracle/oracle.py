@@ -63,6 +63,8 @@ def lib():
         L.co_ang2pix_ring.argtypes = [_I64, _D, _D]
         L.co_pix2ang_ring.restype = None
         L.co_pix2ang_ring.argtypes = [_I64, _I64, _P, _P]
+        L.co_healpix_maps.restype = _I
+        L.co_healpix_maps.argtypes = [_I64, _P, _P, _I, _I, _P, _D, _I, _I, _P]
         L.co_ring_info.restype = None
         L.co_ring_info.argtypes = [_I64, _I64, _P, _P]
         L.co_bin_points.restype = _I
@@ -233,6 +235,59 @@ def sfb_healpix(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, store_
     if rc == 2:
         raise ValueError("argument (z) outside of defined range.")
     return k, c, _unpack_f(fre, fim, lmax, nmax) if store_flmn else []
+
+
+def sfb_healpix_fft(nside, offsets, r_sorted, lmax, nmax, rmax, interpolated, nthreads=0):
+    """HEALPix SFB decomposition with each ring's transform as an FFT, the way the
+    reference computes it (sfb_reverse_fft.cpp:43-209: an FFTW r2c transform per ring;
+    numpy's rfft here, rings of one length transformed together), with the same pixel
+    maps (co_healpix_maps), the same m-extraction without conjugation (s = N/2 -
+    |N/2 - m mod N|, imaginary part dropped at m = 0), ring phase and normalisation as
+    sfb_healpix, the direct-DFT restatement it reproduces to rounding.  Returns
+    (k_ln, c_ln, f_lmn) with f_lmn[l] of shape (l + 1, nmax)."""
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    r_sorted = np.ascontiguousarray(r_sorted, dtype=np.float64)
+    npix, nrings = 12 * nside * nside, 4 * nside - 1
+    k = compute_kln(lmax, nmax, rmax)
+    npts = int(offsets[npix])
+    norm = np.sqrt(2.0 / np.pi) * (4.0 / 3.0) * np.pi * rmax ** 3 / npts
+    starts = np.zeros(nrings, dtype=np.int64)
+    lens = np.zeros(nrings, dtype=np.int64)
+    for i in range(nrings):
+        st, ln = ctypes.c_int64(), ctypes.c_int64()
+        lib().co_ring_info(int(nside), i + 1, ctypes.byref(st), ctypes.byref(ln))
+        starts[i], lens[i] = st.value, ln.value
+    th, ph0 = pix2ang_ring(nside, starts)
+    costh = np.cos(th)
+    groups = {}
+    for i in range(nrings):
+        groups.setdefault(int(lens[i]), []).append(i)
+    c = np.zeros((lmax, nmax))
+    f = []
+    maps = np.zeros((npix, max(nmax, 1)))
+    for l in range(lmax):
+        krow = np.ascontiguousarray(k[l])
+        rc = lib().co_healpix_maps(int(npix), _ptr(offsets), _ptr(r_sorted), int(l), int(nmax), _ptr(krow),
+                                   float(rmax), int(bool(interpolated)), int(nthreads), _ptr(maps))
+        if rc == 2:
+            raise ValueError("argument (z) outside of defined range.")
+        y = np.empty((nrings, l + 1), dtype=np.complex128)
+        for i in range(nrings):
+            for m in range(l + 1):
+                y[i, m] = sph_plm(l, m, costh[i]) * np.exp(-1j * m * ph0[i])
+        acc = np.zeros((l + 1, nmax), dtype=np.complex128)
+        for n_len, ridx in groups.items():
+            ridx = np.asarray(ridx)
+            block = np.stack([maps[starts[i]:starts[i] + n_len, :nmax] for i in ridx])  # (R, N, nmax)
+            spec = np.fft.rfft(block, axis=1)                                          # F[s] = sum_j x_j e^{-2 pi i j s / N}
+            mm = np.arange(l + 1) % n_len
+            val = spec[:, n_len // 2 - np.abs(n_len // 2 - mm), :]                    # (R, l + 1, nmax)
+            val[:, 0, :] = val[:, 0, :].real                                           # sign 0 at m = 0
+            acc += np.einsum("rmn,rm->mn", val, y[ridx])
+        f.append(acc * k[l][None, :] * norm)
+        sq = np.sum(np.abs(acc) ** 2, axis=0)
+        c[l] = (2.0 * sq - np.abs(acc[0]) ** 2) * (norm * k[l]) ** 2 / (2 * l + 1)
+    return k, c, f
 
 
 def ingest(records, cartesian=False, tophat_r0=0.0, gauss_r0=0.0, window=None, window_range=(0.0, 1.0), mask=None,

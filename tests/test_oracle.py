@@ -178,6 +178,21 @@ def test_reverse_equals_fft_path_away_from_aliasing():
         assert np.max(np.abs(f1[l] - f2[l])) <= 1e-12 * np.max(np.abs(f2[l]))
 
 
+@pytest.mark.parametrize("nside,n,lmax,nmax,interp", [(2, 1500, 8, 4, True), (8, 3000, 40, 12, True),
+                                                       (8, 800, 12, 5, False)])
+def test_healpix_fft_restatement_equals_direct(nside, n, lmax, nmax, interp):
+    """The FFT form of the HEALPix oracle (per-ring r2c transforms, as the reference
+    computes them) equals the direct-DFT restatement, aliased frequencies included."""
+    pts = uniform_ball(n, 500.0, seed=nside)
+    offs, rs = O.bin_points(nside, pts)
+    k1, c1, f1 = O.sfb_healpix(nside, offs, rs, lmax, nmax, 500.0, interpolated=interp)
+    k2, c2, f2 = O.sfb_healpix_fft(nside, offs, rs, lmax, nmax, 500.0, interpolated=interp)
+    assert np.array_equal(k1, k2)
+    fmax = max(np.abs(x).max() for x in f1)
+    assert max(np.abs(a - b).max() for a, b in zip(f1, f2)) <= 1e-13 * fmax
+    assert np.allclose(c2, c1, rtol=1e-12, atol=0)
+
+
 def test_oracle_ingest_filters():
     """Ingest restatement: conversion as Point(x, y, z); the tophat keeps exactly r < R0;
     the Gaussian window keeps a fraction matching its expectation; the mask keeps
