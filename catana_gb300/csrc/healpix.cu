@@ -18,8 +18,9 @@
 //               m mod rpix > rpix/2 it uses F[rpix - m mod rpix] itself; the
 //               CATANA_HEALPIX_CONJ_FIX flag conjugates it.  Times Y_lm(ring) -> per-ring
 //               partial sums [ring][m][n]
-//   k_hp_reduce sum over rings (interleaved per warp, fixed order); C_ln = (2 sum_m |f|^2 - |f_0|^2)
-//               (norm k)^2 / (2l+1) and f stored as f k norm (sfb_reverse_fft.cpp:147-153)
+//   k_hp_reduce sum over rings (interleaved per warp, fixed order);
+//               C_ln = (2 sum_m |f|^2 - |f_0|^2) (norm k)^2 / (2l+1) and f stored as
+//               f k norm (sfb_reverse_fft.cpp:147-153)
 // The ring transform: rings whose length is a power of two (all equatorial rings when
 // nside is one, and the polar rings of 4, 8, 16, ... pixels) take a batched FP64 FFT
 // (k_hp_fft: two radial orders packed as one complex sequence, radix-4 passes in
