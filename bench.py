@@ -204,26 +204,8 @@ def side_workloads(torch, _lib, catana, sp):
                                      "kernel_k_fp64_raw_l_tflops": kfl.value / (kms.value / 1e3) / 1e12,
                                      "fp64_peak_note": "nominal GB300 FP64 1.25 TFLOP/s"}
     # HEALPix
-    rng = np.random.default_rng(1)
-    n, R = 1000000, 1000.0
-    nu = int(0.9 * n)
-    nc = n - nu
-
-    def ball(k):
-        r = R * rng.random(k) ** (1 / 3)
-        ct = rng.uniform(-1, 1, k)
-        ph = rng.uniform(0, 2 * np.pi, k)
-        st = np.sqrt(1 - ct ** 2)
-        return np.stack([r * st * np.cos(ph), r * st * np.sin(ph), r * ct], 1)
-    xyz = [ball(nu)]
-    cen = ball(1000)
-    got = 0
-    while got < nc:
-        p = cen[rng.integers(0, 1000, nc)] + rng.normal(0, 5.0, (nc, 3))
-        p = p[np.sum(p ** 2, 1) < R ** 2][:nc - got]
-        xyz.append(p)
-        got += p.shape[0]
-    pc = catana.PointContainer(np.concatenate(xyz), "cartesian")
+    R = HP_RADIUS
+    pc = catana.PointContainer(healpix_catalog(), "cartesian")
     catana.PixelizedPointContainer(256, pc)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -242,6 +224,50 @@ def side_workloads(torch, _lib, catana, sp):
                                                    "for the power-of-two rings (the 513 equatorial rings of "
                                                    "1024 pixels and 16 polar ones), direct sums over quarter-orbits for the rest"}
     return res
+
+
+HP_RADIUS = 1000.0
+
+
+def healpix_catalog(n=1_000_000, seed=1):
+    """Cartesian positions: 90% uniform in a ball of radius 1000, 10% in 1000 Gaussian
+    clumps of sigma 5 (centres uniform in the ball), clipped to the ball."""
+    rng = np.random.default_rng(seed)
+    nu = int(0.9 * n)
+    nc = n - nu
+
+    def ball(k):
+        r = HP_RADIUS * rng.random(k) ** (1 / 3)
+        ct = rng.uniform(-1, 1, k)
+        ph = rng.uniform(0, 2 * np.pi, k)
+        st = np.sqrt(1 - ct ** 2)
+        return np.stack([r * st * np.cos(ph), r * st * np.sin(ph), r * ct], 1)
+    xyz = [ball(nu)]
+    cen = ball(1000)
+    got = 0
+    while got < nc:
+        p = cen[rng.integers(0, 1000, nc)] + rng.normal(0, 5.0, (nc, 3))
+        p = p[np.sum(p ** 2, 1) < HP_RADIUS ** 2][:nc - got]
+        xyz.append(p)
+        got += p.shape[0]
+    return np.concatenate(xyz)
+
+
+def cpu_healpix_baseline(lsample=8):
+    """The HEALPix decomposition's CPU restatement with one r2c FFT per ring, as the
+    reference computes it (oracle.sfb_healpix_fft: pixel maps in C over all host
+    threads, numpy's rfft), on the same catalog binned at nside 256 with nmax 64 and the
+    first `lsample` multipoles.  Its work per multipole (the maps over every point and
+    radial order, the transforms of every ring) does not grow with l, so the lmax 128
+    figure is the sample's time x 128 / lsample."""
+    from oracle import oracle as O
+    pts = O.cartesian_to_spherical(healpix_catalog())
+    offs, rs = O.bin_points(256, pts)
+    t0 = time.perf_counter()
+    O.sfb_healpix_fft(256, offs, rs, lsample, 64, HP_RADIUS, interpolated=True)
+    dt = time.perf_counter() - t0
+    return {"value": dt * 128 / lsample, "unit": "s (lmax 128, scaled)", "cores": os.cpu_count(), "kind": "port",
+            "sample": "lmax %d of 128 on the same 1M points, nside 256, nmax 64: %.1f s" % (lsample, dt)}
 
 
 def batched_workload(torch, _lib, catana, sp, ncat=64, seed=4, kmax=0.2, nmax=128):
@@ -716,6 +742,10 @@ def main():
         v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
         if a.side:
             out["side"]["next_rows"]["shot_noise_integrals_l32_n32"]["cpu_baseline"] = cpu_integrals_baseline()
+            try:
+                out["side"]["healpix_nside256_1M_l128_n64"]["cpu_baseline"] = cpu_healpix_baseline()
+            except Exception as ex:  # a side measurement: never costs the main line
+                out["side"]["healpix_nside256_1M_l128_n64"]["cpu_baseline"] = {"error": repr(ex)}
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                "sample": "%d points (of %d), same lmax/nmax/rmax/weights, interpolated j_l as the "
                                          "reference uses for N > 1000; %.1f s" % (cs, a.points, dt)}
