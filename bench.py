@@ -742,6 +742,15 @@ def main():
         v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
         if a.side:
             out["side"]["next_rows"]["shot_noise_integrals_l32_n32"]["cpu_baseline"] = cpu_integrals_baseline()
+            try:  # the FP64 drop-in case in full: 100k points, lmax = nmax = 32, unit weights, seed 0
+                p1, _ = catalog(100000, 1000.0, 0)
+                v1, t1 = cpu_baseline(p1, None, 32, 32, 1000.0)
+                out["side"]["plain_fp64_100k_l32_n32"]["cpu_baseline"] = {
+                    "value": v1, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                    "sample": "the whole workload (100k points), interpolated j_l as the reference uses for "
+                              "N > 1000; %.2f s" % t1}
+            except Exception as ex:  # a side measurement: never costs the main line
+                out["side"]["plain_fp64_100k_l32_n32"]["cpu_baseline"] = {"error": repr(ex)}
             try:
                 out["side"]["healpix_nside256_1M_l128_n64"]["cpu_baseline"] = cpu_healpix_baseline()
             except Exception as ex:  # a side measurement: never costs the main line
