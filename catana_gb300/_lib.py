@@ -27,7 +27,7 @@ _I32 = ctypes.c_int32
 # status codes (catana_status_t)
 OK, ERR_ARG, ERR_DOMAIN, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED = range(6)
 # flags
-JL_AUTO, JL_INTERP, JL_EXACT = 0, 1, 2
+JL_AUTO, JL_INTERP, JL_EXACT, JL_POLY = 0, 1, 2, 3
 FORM_PLAIN, FORM_SPLIT = 0, 4
 HEALPIX_CONJ_FIX = 8
 BATCH_NO_GRAPH = 16
@@ -77,6 +77,7 @@ SIGNATURES = {
     "catana_gpu_compute_kln": (ctypes.c_int, [_U16, _U16, _D, _P]),
     "catana_gpu_sbessel_integrals": (ctypes.c_int, [_P, _I64, _D, _D, _U32, _D, _P, _P, _I64, _P, _P]),
     "catana_gpu_last_error": (ctypes.c_char_p, []),
+    "catana_gpu_fp64_peak": (ctypes.c_int, [ctypes.c_int32, _P]),
     "catana_gpu_profile_enable": (None, [ctypes.c_int]),
     "catana_gpu_profile_report": (ctypes.c_int, [_P, _P, _P]),
     "catana_gpu_launch_count": (ctypes.c_uint64, []),

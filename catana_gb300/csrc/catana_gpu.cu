@@ -212,6 +212,12 @@ bool resolve_interp(uint32_t flags, int64_t npoints) {
     return npoints > 1000;  // sfb_decomposition.cpp:17 (BESSELINTERPOLATIONPOINTS_PER_ZERO)
 }
 
+// j_l mode of the raw FP64 path: the reference's rule, or the polynomial tables
+JlMode resolve_jl(uint32_t flags, int64_t npoints) {
+    if ((flags & CATANA_JL_MASK) == CATANA_JL_POLY) return JL_MODE_POLY;
+    return resolve_interp(flags, npoints) ? JL_MODE_LERP : JL_MODE_EXACT;
+}
+
 catana_status_t check_args(int64_t npoints, uint16_t lmax, uint16_t nmax, double rmax) {
     if (npoints < 0) {
         set_error("npoints must be >= 0");
@@ -266,7 +272,7 @@ catana_status_t raw_device(DeviceContext *ctx, const double *pts_d, const double
         }
         s = split_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, rmax, kln_d, facc, err_d, st);
     } else {
-        s = fp64_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, resolve_interp(flags, npoints), kln_d, facc,
+        s = fp64_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, resolve_jl(flags, npoints), kln_d, facc,
                                 err_d, st);
     }
     if (s != CATANA_OK) return s;
@@ -283,6 +289,22 @@ catana_status_t raw_device(DeviceContext *ctx, const double *pts_d, const double
     // an empty catalog divides by zero like the reference (f = 0 * inf = NaN)
     const double nf = norm_factor(rmax, wsum);
     return finish_flmn_cln(facc, nf, lmax, nmax, cln_d, st);
+}
+
+// FP64 FMA throughput: 8 independent dependent chains per thread (the result feeds a
+// conditional store so no chain can be dropped).
+__global__ void k_fp64_fma_chains(int iters, double b, double c, double *sink) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t += a[k];
+    if (t == 1234.5) *sink = t;
 }
 
 // Zero the f entries of modes with k_ln > kmax (plain form of the kmax cut).
@@ -372,7 +394,7 @@ catana_status_t batched_device(DeviceContext *ctx, const catana_catalog_t *cats,
         for (int c = 0; c < ncat; ++c) {
             const catana_catalog_t &C = cats[c];
             s = fp64_raw_accumulate(ctx, C.points, C.weights, C.npoints, C.lmax, C.nmax,
-                                    resolve_interp(flags, C.npoints), C.k_ln, facc[c], err_d, st);
+                                    resolve_jl(flags, C.npoints), C.k_ln, facc[c], err_d, st);
             if (s != CATANA_OK) return s;
             if (C.kmax > 0.0 && C.lmax > 0 && C.nmax > 0) {
                 k_kcut<<<dim3(ceil_div((int64_t)C.lmax * C.nmax, 256), C.lmax), 256, 0, st>>>(
@@ -451,6 +473,50 @@ catana_status_t catana_gpu_profile_report(double *kernel_ms, uint64_t *launches,
     if (kernel_ms) *kernel_ms = ms;
     if (launches) *launches = n;
     if (algo_flops) *algo_flops = fl;
+    return CATANA_OK;
+}
+
+catana_status_t catana_gpu_fp64_peak(int32_t ms, double *tflops) {
+    if (!tflops || ms < 1) {
+        set_error("fp64_peak: ms >= 1 and a result pointer are required");
+        return CATANA_ERR_ARG;
+    }
+    int cs;
+    DeviceContext *ctx = get_context(&cs);
+    if (!ctx) return (catana_status_t)cs;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CG_CUDA_TRY(ctx->misc.ensure(256));
+    double *sink = reinterpret_cast<double *>(ctx->misc.as<char>() + 128);
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0, e1;
+    CG_CUDA_TRY(cudaEventCreate(&e0));
+    CG_CUDA_TRY(cudaEventCreate(&e1));
+    const int blocks = 8 * ctx->sm_count, threads = 256;
+    auto timed = [&](int iters, float *msec) -> cudaError_t {
+        cudaEventRecord(e0, st);
+        k_fp64_fma_chains<<<blocks, threads, 0, st>>>(iters, 0.9999999999, 1e-10, sink);
+        count_launch();
+        cudaEventRecord(e1, st);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventElapsedTime(msec, e0, e1);
+        return e;
+    };
+    float t = 0.f;
+    cudaError_t e = timed(2000, &t);  // calibration (and warm-up)
+    double best = 0.0;
+    if (e == cudaSuccess) {
+        const int iters = std::max(2000, (int)(2000.0 * (ms / 3.0) / std::max(1e-3, (double)t)));
+        for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+            e = timed(iters, &t);
+            const double fl = 2.0 * 8.0 * (double)iters * blocks * threads;
+            if (e == cudaSuccess && t > 0.f) best = std::max(best, fl / (t * 1e-3) / 1e12);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CG_CUDA_TRY(e);
+    *tflops = best;
     return CATANA_OK;
 }
 
@@ -767,6 +833,10 @@ catana_status_t catana_gpu_sfb_healpix(int64_t nside, const int64_t *pix_offsets
                                        double *c_ln, double *f_lmn, catana_gpu_stream_t stream) {
     if (nside < 1 || (nside & (nside - 1)) != 0) {
         set_error("argument (nside) must be a power of 2");
+        return CATANA_ERR_ARG;
+    }
+    if ((flags & CATANA_JL_MASK) == CATANA_JL_POLY) {
+        set_error("the pixelized path takes the table or exact j_l, not CATANA_JL_POLY");
         return CATANA_ERR_ARG;
     }
     const int64_t npix = 12 * nside * nside;

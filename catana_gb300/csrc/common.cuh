@@ -82,10 +82,15 @@ struct DeviceContext {
     cudaEvent_t split_ws_event = nullptr;       // end of the last split run (orders workspace reuse across streams)
     DevBuf hp_ws;      // HEALPix workspace
     DevBuf ingest_ws;  // ingest: converted records, keep flags, block counts, window, mask
+    // kernels whose shared-memory limit this device's context has raised (the
+    // attribute is per device, so it is tracked here rather than per process)
+    bool attr_fp64 = false, attr_split = false, attr_healpix = false;
     // cache keys
     int coef_lmax = -1;
     int tab_lmax = -1, tab_nmax = -1;
     std::vector<double> tab_dxinv, tab_zmax;  // per l
+    DevBuf poly;       // piecewise FP64 j_l polynomials [l][interval][12] (CATANA_JL_POLY)
+    int poly_lmax = -1, poly_nint = -1;
 };
 
 DeviceContext *get_context(int *status);
@@ -106,10 +111,14 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
         }                                                                                        \
     } while (0)
 
+// j_l evaluation of the FP64 plain path: the reference's linear table, the direct
+// evaluation, or the piecewise FP64 polynomials (CATANA_JL_POLY).
+enum JlMode { JL_MODE_LERP = 0, JL_MODE_EXACT = 1, JL_MODE_POLY = 2 };
+
 // FP64 plain raw path (sfb_fp64.cu).  All pointers device.  Accumulates into
 // f_acc (complex, packed by l, un-normalised); the caller normalises.
 catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
-                                    int64_t npoints, int lmax, int nmax, bool interpolated, const double *kln_dev,
+                                    int64_t npoints, int lmax, int nmax, JlMode jl, const double *kln_dev,
                                     double *f_acc_dev, int *err_dev, cudaStream_t st);
 // f *= norm; c_ln from f (device).
 catana_status_t finish_flmn_cln(double *f_dev, double norm, int lmax, int nmax, double *c_ln_dev,

@@ -664,12 +664,11 @@ catana_status_t healpix_sfb_dev(DeviceContext *ctx, int64_t nside, const int64_t
     const int npts_tab = 1000 * nmax;
     const size_t smem = (2 * HP_MAXPIX + 4 * HP_JC * HP_NB) * sizeof(double);
     const size_t smem_fft = (size_t)HF_G * R.max_pow2 * sizeof(double2);
-    static bool attr = false;
-    if (!attr) {
+    if (!ctx->attr_healpix) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_hp_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CG_CUDA_TRY(cudaFuncSetAttribute(k_hp_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(HF_G * HP_MAXPIX * sizeof(double2))));
-        attr = true;
+        ctx->attr_healpix = true;
     }
     for (int l = 0; l < lmax; ++l) {
         // the level is in the table's range when 0 <= r_min and k_max r_max < zmax (NaN radii fail both)

@@ -2,6 +2,12 @@
 // ApJ 622:759, sec. 4), every product and sum rounded separately in the operation
 // order of the CPU restatement, so both give the same pixel.  Shared by the binning,
 // the pixelized SFB and the on-device ingest (angular masks).
+// Source of the operation order: the reference bins with HEALPix C++
+// (Healpix_Base::loc2pix / pix2loc in Healpix_cxx/healpix_base.cc, GPL-2), and a
+// bit-exact pixel needs that implementation's branches -- the sin(theta) path for
+// theta within 0.01 of a pole, the za < 0.99 polar test, and the integer
+// kshift / (t1 >> 1) & (4 nside - 1) arithmetic of the equatorial belt -- which the
+// paper does not spell out.  They are restated here, not copied.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -12,8 +12,10 @@
 //   * e^{-im phi} comes from one sincospi of the exactly reduced phase frac(m u) per
 //     thread and m-run plus complex rotation by e^{i phi} (prepared once per point);
 //   * j_l comes from the reference's own linear table (1000*nmax nodes up to
-//     z_{l,nmax}, same node placement, same dx_inv, same lerp) or, in exact mode,
-//     from the direct evaluation in special.cuh;
+//     z_{l,nmax}, same node placement, same dx_inv, same lerp), in exact mode from
+//     the direct evaluation in special.cuh, or (CATANA_JL_POLY, no counterpart in the
+//     reference) from piecewise FP64 polynomials of degree 11 on unit intervals of
+//     z = k r, within ~1e-14 of j_l's envelope at the cost of a table lookup;
 //   * a CTA owns a slab of points and a TILE x TILE block of (m, n); it stages
 //     J[n][pt] and Y[m][pt] for 32 points in shared memory and accumulates f(m,n) in
 //     FP64 registers (TILE/16 x TILE/16 complex per thread);
@@ -26,6 +28,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -73,13 +76,83 @@ __global__ void k_lerp_tables(double *__restrict__ tab, const double *__restrict
     tab[t] = sbessel_jl(l, 0.0 + (double)(size_t)i * dx[l]);
 }
 
+// ---- piecewise FP64 j_l polynomials (CATANA_JL_POLY) ----
+// Interval j covers z in [j - 1/2, j + 1/2]; on it j_l(z) = sum_s a_s t^s, t = 2 (z - j),
+// the monomial form of the degree-11 Chebyshev interpolant through 12 Chebyshev
+// nodes.  Chebyshev interpolation of an entire function of bounded derivatives on a
+// unit interval errs by <= 2 (1/4)^12 / 12! max |j_l^(12)| ~ 1e-16 of the envelope, so
+// the FP64 node values (special.cuh, ~1e-14) bound the accuracy.
+constexpr int kPolyNC = 12;
+
+__host__ __device__ inline double poly_node(int k) {
+    return cos((2.0 * k + 1.0) * kPi / (2.0 * kPolyNC));
+}
+
+// vals[node][l] = j_l(z_node) for every l < lmax (node = 12 j + k)
+__global__ void k_poly_nodes(int lmax, int nint, double *vals) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nint * kPolyNC) return;
+    const int j = node / kPolyNC, k = node - kPolyNC * j;
+    const double z = (double)j + 0.5 * poly_node(k);
+    double *o = vals + (size_t)node * lmax;
+    sbessel_jl_all(lmax, fabs(z), o);
+    if (z < 0.0)  // the first interval straddles 0: j_l(-z) = (-1)^l j_l(z)
+        for (int l = 1; l < lmax; l += 2) o[l] = -o[l];
+}
+
+// Chebyshev coefficients c_r = (2/12) sum_k f_k T_r(t_k) (c_0 halved), then the
+// monomial coefficients a_s = sum_r c_r [t^s] T_r(t) (cheb2mono, row-major [s][r]).
+// The two steps keep the large entries of the basis change away from the node values:
+// they multiply only the small high-order c_r.
+__global__ void k_poly_coefs(int lmax, int nint, const double *__restrict__ vals,
+                             const double *__restrict__ cheb2mono, double *__restrict__ tab) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= lmax * nint) return;
+    const int l = t / nint, j = t - l * nint;
+    double f[kPolyNC], c[kPolyNC];
+    for (int k = 0; k < kPolyNC; ++k) f[k] = vals[(size_t)(kPolyNC * j + k) * lmax + l];
+    for (int r = 0; r < kPolyNC; ++r) {
+        double acc = 0.0;
+        for (int k = 0; k < kPolyNC; ++k) acc += f[k] * cospi((double)(r * (2 * k + 1)) / (2.0 * kPolyNC));
+        c[r] = acc * (r == 0 ? 1.0 : 2.0) / kPolyNC;
+    }
+    double *o = tab + ((size_t)l * nint + j) * kPolyNC;
+    for (int s2 = 0; s2 < kPolyNC; ++s2) {
+        double acc = 0.0;
+        for (int r = kPolyNC - 1; r >= s2; --r) acc += cheb2mono[s2 * kPolyNC + r] * c[r];
+        o[s2] = acc;
+    }
+}
+
+// max r over the catalog (IEEE bits of a non-negative double) and a flag for a
+// negative or non-finite radius
+__global__ void k_fp64_maxr(const double *__restrict__ pts, int64_t n, unsigned long long *out) {
+    double mr = 0.0;
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double r = pts[3 * i];
+        if (!(r >= 0.0) || !isfinite(r)) bad = true;
+        else if (r > mr) mr = r;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        bad |= __shfl_xor_sync(0xffffffffu, (int)bad, o) != 0;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(mr));
+        if (bad) atomicMax(&out[1], 1ull);
+    }
+}
+
 struct LArgs {
     int l, nmax, nslabs;
     int64_t n;  // points in the chunk
     const double *r, *x, *w, *c1, *s1;
     const unsigned long long *u;  // phase fractions frac(phi / 2 pi) 2^64
     const double *kln;  // k_ln row of l (nmax)
-    const double *tab;  // lerp table of l, or null for exact j_l
+    const double *tab;  // lerp table of l, or null
+    const double *poly; // FP64 polynomial table of l ([interval][12]), or null (exact j_l when both are null)
+    int poly_nint;
     int npts_tab;
     double dx_inv, zmax;
     const double *st1, *st2;  // P_{l-1}^m, P_{l-2}^m rows: [m][n]
@@ -159,6 +232,27 @@ __global__ void __launch_bounds__(kThreads) k_fp64_raw_l(LArgs a) {
                         const double y0 = a.tab[ii], y1 = a.tab[ii + 1];
                         j = y0 + (y1 - y0) * (ia - ii);
                     }
+                } else if (a.poly) {
+                    const double zr = rint(z);
+                    int jj = (int)zr;
+                    if (!(z >= 0.0) || jj >= a.poly_nint) {  // the host sized the table from max r
+                        *a.err = CATANA_ERR_DOMAIN;
+                        jj = 0;
+                    }
+                    const double t = 2.0 * (z - zr);
+                    const double2 *c2 = reinterpret_cast<const double2 *>(a.poly + (size_t)jj * kPolyNC);
+                    const double2 c45 = c2[5], c34 = c2[4], c23 = c2[3], c12 = c2[2], c01 = c2[1], c00 = c2[0];
+                    double p = fma(c45.y, t, c45.x);
+                    p = fma(p, t, c34.y);
+                    p = fma(p, t, c34.x);
+                    p = fma(p, t, c23.y);
+                    p = fma(p, t, c23.x);
+                    p = fma(p, t, c12.y);
+                    p = fma(p, t, c12.x);
+                    p = fma(p, t, c01.y);
+                    p = fma(p, t, c01.x);
+                    p = fma(p, t, c00.y);
+                    j = fma(p, t, c00.x);
                 } else {
                     j = sbessel_jl(l, z);
                 }
@@ -340,9 +434,48 @@ catana_status_t ensure_lerp_tables(DeviceContext *ctx, int lmax, int nmax, cudaS
     return CATANA_OK;
 }
 
+// FP64 j_l polynomials for l < lmax over nint unit intervals (cached per device; a
+// larger cached table serves, with its own interval count as the row stride)
+catana_status_t ensure_poly_tables(DeviceContext *ctx, int lmax, int nint, cudaStream_t st) {
+    if (ctx->poly_lmax >= lmax && ctx->poly_nint >= nint) return CATANA_OK;
+    lmax = std::max(lmax, ctx->poly_lmax);
+    nint = std::max(nint, ctx->poly_nint);
+    // [t^s] T_r(t) by T_{r+1} = 2 t T_r - T_{r-1} (exact small integers)
+    std::vector<double> T((size_t)kPolyNC * kPolyNC, 0.0), m2((size_t)kPolyNC * kPolyNC, 0.0);
+    T[0] = 1.0;                 // T_0 = 1   (row r, column s)
+    T[kPolyNC + 1] = 1.0;       // T_1 = t
+    for (int r = 1; r + 1 < kPolyNC; ++r)
+        for (int s2 = 0; s2 < kPolyNC; ++s2) {
+            const double up = s2 > 0 ? 2.0 * T[(size_t)r * kPolyNC + s2 - 1] : 0.0;
+            T[(size_t)(r + 1) * kPolyNC + s2] = up - T[(size_t)(r - 1) * kPolyNC + s2];
+        }
+    for (int s2 = 0; s2 < kPolyNC; ++s2)
+        for (int r = 0; r < kPolyNC; ++r) m2[(size_t)s2 * kPolyNC + r] = T[(size_t)r * kPolyNC + s2];
+    const size_t tab_bytes = (size_t)lmax * nint * kPolyNC * sizeof(double);
+    CG_CUDA_TRY(ctx->poly.ensure(tab_bytes));
+    DevBuf tmp;
+    const size_t vbytes = (size_t)nint * kPolyNC * lmax * sizeof(double);
+    CG_CUDA_TRY(tmp.ensure(vbytes + m2.size() * sizeof(double)));
+    double *vals = tmp.as<double>();
+    double *m2d = vals + (size_t)nint * kPolyNC * lmax;
+    CG_CUDA_TRY(cudaMemcpyAsync(m2d, m2.data(), m2.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_poly_nodes<<<ceil_div((int64_t)nint * kPolyNC, 64), 64, 0, st>>>(lmax, nint, vals);
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    k_poly_coefs<<<ceil_div((int64_t)lmax * nint, 128), 128, 0, st>>>(lmax, nint, vals, m2d, ctx->poly.as<double>());
+    count_launch();
+    CG_CUDA_TRY(cudaGetLastError());
+    CG_CUDA_TRY(cudaStreamSynchronize(st));
+    tmp.release();
+    ctx->poly_lmax = lmax;
+    ctx->poly_nint = nint;
+    return CATANA_OK;
+}
+
 catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
-                                    int64_t npoints, int lmax, int nmax, bool interpolated, const double *kln_dev,
+                                    int64_t npoints, int lmax, int nmax, JlMode jl, const double *kln_dev,
                                     double *f_acc_dev, int *err_dev, cudaStream_t st) {
+    const bool interpolated = (jl == JL_MODE_LERP);
     catana_status_t s = ensure_coefs(ctx, lmax, st);
     if (s != CATANA_OK) return s;
     if (interpolated) {
@@ -350,6 +483,36 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
         if (s != CATANA_OK) return s;
     }
     if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
+    if (jl == JL_MODE_POLY) {
+        // the table must reach max_l k_{l,nmax-1} * max r: one read-back of max r
+        CG_CUDA_TRY(ctx->cat_scratch.ensure(16));
+        unsigned long long *mx = ctx->cat_scratch.as<unsigned long long>();
+        CG_CUDA_TRY(cudaMemsetAsync(mx, 0, 16, st));
+        k_fp64_maxr<<<std::min<int64_t>(4 * ctx->sm_count, ceil_div(npoints, 256)), 256, 0, st>>>(points_dev, npoints,
+                                                                                                  mx);
+        count_launch();
+        CG_CUDA_TRY(cudaGetLastError());
+        unsigned long long mh[2] = {0ull, 0ull};
+        std::vector<double> kh((size_t)lmax * nmax);
+        CG_CUDA_TRY(cudaMemcpyAsync(mh, mx, 16, cudaMemcpyDeviceToHost, st));
+        CG_CUDA_TRY(cudaMemcpyAsync(kh.data(), kln_dev, kh.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CG_CUDA_TRY(cudaStreamSynchronize(st));
+        double max_r;
+        memcpy(&max_r, &mh[0], 8);
+        if (mh[1]) {
+            set_error("argument (z) outside of defined range: a radius is negative or not finite");
+            return CATANA_ERR_DOMAIN;
+        }
+        double kmax = 0.0;
+        for (double k : kh) kmax = std::max(kmax, k);
+        const double zmax = kmax * max_r;
+        if (!(zmax < 1e6)) {
+            set_error("poly j_l: k_ln * max(r) beyond 1e6");
+            return CATANA_ERR_DOMAIN;
+        }
+        s = ensure_poly_tables(ctx, lmax, (int)std::floor(zmax + 0.5) + 2, st);
+        if (s != CATANA_OK) return s;
+    }
     // Chunk so that the three Legendre rows stay under ~1.5 GB.
     int64_t chunk = (int64_t)(1.5e9 / (3.0 * 8.0 * std::max(lmax, 1)));
     chunk = std::max<int64_t>(1024, std::min<int64_t>(chunk, npoints));
@@ -371,11 +534,10 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
         }
         CG_CUDA_TRY(ctx->partial.ensure(pmax));
     }
-    static bool attr_set = false;
-    if (!attr_set) {
+    if (!ctx->attr_fp64) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_fp64_raw_l<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(3 * kTP * (64 + 1) * sizeof(double))));
-        attr_set = true;
+        ctx->attr_fp64 = true;
     }
 
     for (int64_t c0 = 0; c0 < npoints; c0 += chunk) {
@@ -406,6 +568,8 @@ catana_status_t fp64_raw_accumulate(DeviceContext *ctx, const double *points_dev
             a.u = uph;
             a.kln = kln_dev + (size_t)l * nmax;
             a.tab = interpolated ? ctx->tables.as<double>() + (size_t)l * npts_tab : nullptr;
+            a.poly = jl == JL_MODE_POLY ? ctx->poly.as<double>() + (size_t)l * ctx->poly_nint * kPolyNC : nullptr;
+            a.poly_nint = ctx->poly_nint;
             a.npts_tab = npts_tab;
             a.dx_inv = interpolated ? ctx->tab_dxinv[l] : 0.0;
             a.zmax = interpolated ? ctx->tab_zmax[l] : 0.0;
@@ -517,6 +681,10 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
         return CATANA_ERR_ARG;
     }
     const uint32_t jl = flags & CATANA_JL_MASK;
+    if (jl == CATANA_JL_POLY) {
+        set_error("sfb_raw_noalloc: the polynomial j_l tables (CATANA_JL_POLY) are not available allocation-free");
+        return CATANA_ERR_ARG;
+    }
     const bool interpolated = jl == CATANA_JL_INTERP || (jl == CATANA_JL_AUTO && npoints > 1000);
     // scratch plan: [words 256 B][coefficients][tables + dx][SoA][3 Legendre rows][partials]
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
@@ -637,6 +805,8 @@ extern "C" catana_status_t catana_gpu_sfb_raw_noalloc(const double *points_dev, 
             a.s1 = s1;
             a.u = uph;
             a.tab = interpolated ? tab_d + (size_t)l * npts_tab : nullptr;
+            a.poly = nullptr;
+            a.poly_nint = 0;
             a.npts_tab = npts_tab;
             a.dx_inv = interpolated ? dxinv[l] : 0.0;
             a.zmax = interpolated ? zmx[l] : 0.0;

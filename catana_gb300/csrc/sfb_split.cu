@@ -32,6 +32,12 @@
 //     representable (enough for lmax <= 256); the m = 0 step is rounded once
 //     (step_once), so Y_l0 carries no mean error over the sphere through which a
 //     catalog's monopole could leak into l > 0;
+//   * the seeds of every m column stay FP64: a per-point FP64 sectoral value P_ll
+//     (double-buffered by the parity of l) advances by P_ll = a_l s P_{l-1,l-1} in
+//     FP64 each level, and both P_ll and P_{l,l-1} = sqrt(2l+1) x P_{l-1,l-1} are
+//     formed from it in FP64 and rounded once into the FP32 rows -- so the FP32
+//     recurrence of column m starts from correctly rounded values at l = m, m + 1
+//     instead of inheriting m rounded sectoral steps;
 //   * e^{-i m phi}: one sincospif of the exact phase (64-bit fixed-point fraction of a
 //     turn) per warp-run of <= 8 m, then complex rotation by e^{i phi}.
 // Pipeline: two operand buffers and two row stages.  Warps 0..15 generate the operands
@@ -95,6 +101,7 @@ constexpr uint32_t OFF_COEF = OFF_INV + NHALF * 4;      // recurrence coefficien
 constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
+constexpr double P00_SCALED_D = 0.28209479177387814347 * 1.2676506002282294e30;
 // Y operand = P * 2^12: the stored rows carry 2^100, so the readout factor is 2^-88.
 // Scaling both operands towards the top of the FP16 range keeps the lo halves normal.
 constexpr float Y_UNSCALE = 3.2311742677852644e-27f;  // 2^-88
@@ -124,6 +131,7 @@ struct SplitCat {
     const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..2, then exponent words of sets 0..2
     const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
+    double *sect;           // FP64 sectoral P_ll 2^100 per point, two sets [l & 1][stride]
 };
 
 // One CTA of a level launch: a catalog, a block of complex m, a range of tiles.
@@ -134,6 +142,7 @@ struct SplitItem {
 
 struct SplitArgs {
     int l, nint;
+    double a_sect, a_sub;    // FP64 seed coefficients of l: -sqrt((2l+1)/(2l)), sqrt(2l+1)
     const SplitItem *items;  // this level's items (one per CTA)
     const SplitCat *cats;
     const float4 *coef;      // recurrence coefficients, row l
@@ -353,6 +362,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
     const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
     float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
+    const double *__restrict__ sect_prev = cat.sect + (size_t)((l + 1) & 1) * stride;  // FP64 P_{l-1,l-1}
+    double *__restrict__ sect_cur = cat.sect + (size_t)(l & 1) * stride;               // FP64 P_ll
     const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
     unsigned long long *ex0 = nullptr;
     if (EXT) {
@@ -697,44 +708,55 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                     if (mlh < mhi) {  // warp-uniform
                                         if (l == 0) {
                                             Pq = P00_SCALED;
-                                        } else {
-                                            const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
-                                            const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
+                                            if (wrows) sect_cur[i] = P00_SCALED_D;
+                                        } else if (mh >= l - 1) {
+                                            // FP64 seeds: P_ll = a_sect s P_{l-1,l-1} and
+                                            // P_{l,l-1} = a_sub x P_{l-1,l-1} from the per-point
+                                            // FP64 sectoral value, rounded once into the row
                                             const bool sect = (mh == l);
-                                            const float p1 = stg1[(sect ? mlh - 1 : mlh) * KT + q];  // sectoral: P_{l-1,l-1}
-                                            const float xa = sect ? sh : xh, xb = sect ? sl : xl;
-                                            float p2 = (mh <= l - 2) ? stg2[mlh * KT + q] : 0.f;
-                                            if (EXT) {  // exponents of P_{l-1} (the sectoral step reads row l-1) and P_{l-2}
-                                                const unsigned long long w1 = stge1[sect ? mlh - 1 : mlh];
-                                                e = (unsigned)((w1 >> q) & 1ull) | ((unsigned)((w1 >> (32 + q)) & 1ull) << 1);
-                                                if (mh <= l - 2) {
-                                                    const unsigned long long w2 = stge2[mlh];
-                                                    const unsigned e2 = (unsigned)((w2 >> q) & 1ull) |
-                                                                        ((unsigned)((w2 >> (32 + q)) & 1ull) << 1);
-                                                    // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                                    if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
-                                                }
-                                            }
-                                            const float tt = fmaf(xa, p1, xb * p1);
-                                            // rounded once (step_once); at l = 2, m = 0 P_{l-2} = P_00
-                                            // is the same for every point, so the fma chain's error
-                                            // would even be one constant shared by all points
-                                            Pq = step_once(A_hi, A_lo, B_hi, B_lo, tt, p2);
-                                            if (EXT) {
-                                                const float ap = fabsf(Pq);
+                                            const double pp = sect_prev[i];
+                                            double v = sect ? a.a_sect * ((double)sh + (double)sl) * pp
+                                                            : a.a_sub * ((double)xh + (double)xl) * pp;
+                                            if (sect && wrows) sect_cur[i] = v;
+                                            if (EXT) {  // the frame of P_{l-1,l-1}: stored value P 2^100 2^(128 e)
+                                                e = ebits(stge1[sect ? mlh - 1 : mlh], q);
+                                                for (unsigned k = 0; k < e; ++k) v *= 0x1p128;
+                                                Pq = (float)v;
                                                 if (sect) {
-                                                    if (ap < 0x1p-40f) {
+                                                    if (fabsf(Pq) < 0x1p-40f) {
                                                         if (e < 3) {
-                                                            Pq = Pq * 0x1p64f * 0x1p64f;
+                                                            Pq = (float)(v * 0x1p128);
                                                             ++e;
                                                         } else {
                                                             Pq = 0.f;  // below 2^-520: no contribution within lmax
                                                         }
                                                     }
-                                                } else if (e > 0 && ap > 0x1p40f) {
-                                                    Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                } else if (e > 0 && fabsf(Pq) > 0x1p40f) {
+                                                    Pq = (float)(v * 0x1p-128);
                                                     --e;
                                                 }
+                                            } else {
+                                                Pq = (float)v;
+                                            }
+                                        } else {  // m <= l - 2: one recurrence step, rounded once
+                                            const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
+                                            const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
+                                            const float p1 = stg1[mlh * KT + q];
+                                            float p2 = stg2[mlh * KT + q];
+                                            if (EXT) {  // exponents of P_{l-1} and P_{l-2}
+                                                e = ebits(stge1[mlh], q);
+                                                const unsigned e2 = ebits(stge2[mlh], q);
+                                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
+                                                if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
+                                            }
+                                            const float tt = fmaf(xh, p1, xl * p1);
+                                            // rounded once (step_once); at l = 2, m = 0 P_{l-2} = P_00
+                                            // is the same for every point, so the fma chain's error
+                                            // would even be one constant shared by all points
+                                            Pq = step_once(A_hi, A_lo, B_hi, B_lo, tt, p2);
+                                            if (EXT && e > 0 && fabsf(Pq) > 0x1p40f) {
+                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                --e;
                                             }
                                         }
                                         if (wrows) rowp[h ? stride : 0] = Pq;
@@ -1162,8 +1184,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         cats.push_back(p);
     }
     if (cats.empty()) return CATANA_OK;
-    static bool attr = false;
-    if (!attr) {
+    if (!ctx->attr_split) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SMEM_BYTES));
         CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1172,7 +1193,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                                          (int)SMEM_BYTES));
         CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SMEM_BYTES));
-        attr = true;
+        ctx->attr_split = true;
     }
     // ---- extents: max r and max |w| per catalog (one synchronisation) ----
     const int nc = (int)cats.size();
@@ -1270,7 +1291,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
         size_t ws_bytes = 0;
-        std::vector<size_t> off_pts(gn), off_rows(gn), off_exp(gn);
+        std::vector<size_t> off_pts(gn), off_rows(gn), off_exp(gn), off_sect(gn);
         for (int c = c0; c < c1; ++c) smax = std::max(smax, cats[c].stride);
         const size_t keyb = al256((size_t)smax * 4), histb = al256((size_t)256 * ((smax + 4095) / 4096 + 1) * 4);
         ws_bytes = 4 * keyb + histb;
@@ -1281,6 +1302,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             ws_bytes += al256((size_t)3 * cats[c].stride * cats[c].in.lmax * sizeof(float));
             off_exp[c - c0] = ws_bytes;
             if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
+            off_sect[c - c0] = ws_bytes;
+            ws_bytes += al256((size_t)2 * cats[c].stride * sizeof(double));
         }
         CG_CUDA_TRY(ctx->split_ws.ensure(ws_bytes));
         char *ws = ctx->split_ws.as<char>();
@@ -1390,6 +1413,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.tmaps = nullptr;  // patched at upload
             sc.kz = nullptr;  // patched below, once the plan buffer's address is known
             sc.nmax_l = nullptr;
+            sc.sect = reinterpret_cast<double *>(ws + off_sect[c - c0]);
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
         // Work items of every level for a schedule of `waves` CTAs per SM: at level l
@@ -1510,6 +1534,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             SplitArgs a;
             a.l = l;
             a.nint = nint_tab;
+            a.a_sect = l >= 1 ? -std::sqrt((2.0 * l + 1.0) / (2.0 * l)) : 0.0;
+            a.a_sub = std::sqrt(2.0 * l + 1.0);
             a.items = reinterpret_cast<const SplitItem *>(pd + o_items) + S.item0[l];
             a.cats = reinterpret_cast<const SplitCat *>(pd + o_cats);
             a.coef = coef_d + (size_t)l * (l + 1) / 2;

@@ -165,7 +165,8 @@ catana_status_t accum_add(Accum *A, const T *points, const T *weights, int64_t n
         // the reference's j_l rule applies to the whole catalog, not to a chunk:
         // JL_AUTO picks the table form here (streamed catalogs are large)
         const uint32_t jl = A->flags & CATANA_JL_MASK;
-        s = fp64_raw_accumulate(ctx, p64, w64, n, A->lmax, A->nmax, jl != CATANA_JL_EXACT, A->kln.as<double>(),
+        const JlMode mode = jl == CATANA_JL_POLY ? JL_MODE_POLY : jl == CATANA_JL_EXACT ? JL_MODE_EXACT : JL_MODE_LERP;
+        s = fp64_raw_accumulate(ctx, p64, w64, n, A->lmax, A->nmax, mode, A->kln.as<double>(),
                                 A->facc.as<double>(), err_d, A->comp_st);
     }
     if (s != CATANA_OK) return s;
@@ -231,7 +232,9 @@ catana_status_t accum_add_records(Accum *A, const void *records, int64_t n, cons
             s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);
         } else {
             const uint32_t jl = A->flags & CATANA_JL_MASK;
-            s = fp64_raw_accumulate(ctx, pts, nullptr, kept, A->lmax, A->nmax, jl != CATANA_JL_EXACT,
+            const JlMode mode =
+                jl == CATANA_JL_POLY ? JL_MODE_POLY : jl == CATANA_JL_EXACT ? JL_MODE_EXACT : JL_MODE_LERP;
+            s = fp64_raw_accumulate(ctx, pts, nullptr, kept, A->lmax, A->nmax, mode,
                                     A->kln.as<double>(), A->facc.as<double>(), err_d, A->comp_st);
         }
         if (s != CATANA_OK) return s;

@@ -12,7 +12,9 @@ Keyword extensions (absent in the reference, defaults reproduce it):
   precision='plain'    'plain': FP64 on CUDA cores (the drop-in);
                        'split': tcgen05 tensor cores, 3-term FP16 hi+lo products
   interpolation='auto' 'auto' (interpolated iff N > 1000, the reference's rule),
-                       'on' (linear table) or 'off' (exact j_l)
+                       'on' (linear table), 'off' (exact j_l) or 'poly' (piecewise
+                       FP64 polynomials, as accurate as 'off' at the cost of 'on';
+                       raw path, plain form)
   conj_fix=False       HEALPix only: conjugate aliased ring coefficients instead of
                        reproducing the reference's unconjugated read.
 """
@@ -25,7 +27,7 @@ import numpy as np
 from . import _lib
 from .basictypes import PixelizedPointContainer, PointContainer
 
-_INTERP = {"auto": _lib.JL_AUTO, "on": _lib.JL_INTERP, "off": _lib.JL_EXACT}
+_INTERP = {"auto": _lib.JL_AUTO, "on": _lib.JL_INTERP, "off": _lib.JL_EXACT, "poly": _lib.JL_POLY}
 _FORM = {"plain": _lib.FORM_PLAIN, "split": _lib.FORM_SPLIT}
 
 

@@ -50,12 +50,21 @@ typedef enum {
 #define CATANA_JL_AUTO 0u
 #define CATANA_JL_INTERP 1u  /* linear table, 1000*nmax nodes up to z_{l,nmax} (SBesselInterpolator.cpp:10-26) */
 #define CATANA_JL_EXACT 2u   /* direct j_l evaluation (the reference's gsl_sf_bessel_jl branch) */
+/* Plain raw path only, no counterpart in the reference: j_l from piecewise FP64
+ * polynomials (degree 11 in Chebyshev form, one per unit interval of z = k r centred
+ * on an integer), within ~1e-14 of the envelope of j_l -- the accuracy of the
+ * exact branch at the cost of the table branch.  It serves as the FP64 reference the
+ * split form is measured against at full catalog sizes.  The healpix and
+ * allocation-free entry points reject it (CATANA_ERR_ARG); negative or non-finite
+ * radii are CATANA_ERR_DOMAIN. */
+#define CATANA_JL_POLY 3u
 #define CATANA_JL_MASK 3u
 /* Contraction form.  PLAIN: FP64 on CUDA cores, the drop-in.  SPLIT: tensor-core
  * tcgen05 contraction of 3-term FP16 hi+lo products with FP32 accumulation,
- * folded per 32-point tile and reduced in FP64; j_l from a piecewise degree-5 table
- * accurate to ~1.2e-7 of its envelope (the JL flags do not apply); lmax <= 256,
- * nmax <= 128. */
+ * folded per 32-point tile and reduced in FP64; j_l from piecewise degree-6
+ * polynomials on unit intervals with FP32 coefficients, accurate to ~1e-7 of its
+ * envelope (the JL flags do not apply); lmax <= 512, nmax <= 256 (above lmax 256
+ * the Legendre rows carry a 2-bit exponent per value). */
 #define CATANA_FORM_PLAIN 0u
 #define CATANA_FORM_SPLIT 4u
 #define CATANA_FORM_MASK 4u
@@ -305,6 +314,12 @@ catana_status_t catana_gpu_compute_kln(uint16_t lmax, uint16_t nmax, double rmax
  * reference (it has no GPU). */
 void catana_gpu_profile_enable(int enable);
 catana_status_t catana_gpu_profile_report(double *kernel_ms, uint64_t *launches, double *algo_flops);
+
+/* FP64 FMA throughput of the current device as its clocks stand (TFLOP/s, 2 flops
+ * per FMA): independent FMA chains, 8 CTAs of 256 threads per SM, about `ms`
+ * milliseconds in three timed launches, the best one reported.  The denominator of
+ * the plain path's roofline.  No counterpart in the reference. */
+catana_status_t catana_gpu_fp64_peak(int32_t ms, double *tflops);
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *catana_gpu_last_error(void);

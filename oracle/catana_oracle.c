@@ -361,7 +361,11 @@ int co_sfb_raw(const double *pts, const double *w, int64_t npoints, int lmax, in
 /* HEALPix RING scheme (nside a power of two), restated from Gorski et al.    */
 /* 2005, ApJ 622:759, section 4 and the HEALPix primer.  The reference calls  */
 /* Healpix_Base::ang2pix / pix2ang / get_ring_info_small                      */
-/* (PixelizedPointContainer.cpp:16-30, sfb_reverse_fft.cpp:78).               */
+/* (PixelizedPointContainer.cpp:16-30, sfb_reverse_fft.cpp:78).  The branch   */
+/* structure and operation order (sin(theta) near the poles, the za < 0.99    */
+/* polar test, kshift and (t1 >> 1) & (nl4 - 1)) follow HEALPix C++'s         */
+/* Healpix_Base::loc2pix / pix2loc (Healpix_cxx/healpix_base.cc, GPL-2), which */
+/* bit-exact pixels need; the paper does not give them.                       */
 /* ------------------------------------------------------------------------- */
 static double co_fmodulo(double v1, double v2)
 {

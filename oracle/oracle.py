@@ -32,12 +32,17 @@ def build(force=False):
         subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
 
 
-def build_ref(ref_root="/root/reference"):
-    """Compile the reference's besseltools sources (needs the reference tree)."""
-    if not os.path.isdir(ref_root):
-        return False
-    subprocess.run(["make", "-s", "-C", _HERE, "ref", "REF=" + ref_root], check=True)
-    return True
+def build_ref(ref_root=None):
+    """Compile the reference's besseltools sources where the reference tree exists.
+    The tree is ref_root, else $CATANA_REFERENCE_DIR, else the recipe's default
+    location (oracle/Makefile, REF); without a tree nothing is built.  Returns
+    whether oracle/_ref holds the library afterwards."""
+    ref_root = ref_root or os.environ.get("CATANA_REFERENCE_DIR")
+    cmd = ["make", "-s", "-C", _HERE, "ref-if-present"]
+    if ref_root:
+        cmd.append("REF=" + ref_root)
+    subprocess.run(cmd, check=True)
+    return os.path.exists(_REF_PATH)
 
 
 def lib():

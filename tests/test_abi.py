@@ -112,6 +112,19 @@ def test_sfb_argument_validation():
         catana.sfb_decomposition(pc, 4, 4, 10.0, precision="half")
 
 
+def test_poly_jl_rejected_where_unsupported():
+    """CATANA_JL_POLY serves the raw path only: the pixelized and allocation-free
+    entry points reject it before touching a device."""
+    offs = np.zeros(12 + 1, dtype=np.int64)
+    k, c = np.zeros(4), np.zeros(4)
+    st = _lib.lib.catana_gpu_sfb_healpix(1, _lib.ptr(offs), None, 2, 2, 10.0, _lib.JL_POLY, _lib.ptr(k),
+                                         _lib.ptr(c), None, None)
+    assert st == _lib.ERR_ARG and "POLY" in _lib.last_error()
+    st = _lib.lib.catana_gpu_sfb_raw_noalloc(None, None, 0, 2, 2, 10.0, _lib.JL_POLY, _lib.ptr(k), _lib.ptr(c),
+                                             _lib.ptr(k), None)
+    assert st == _lib.ERR_ARG and "POLY" in _lib.last_error()
+
+
 def test_savetxt_format(tmp_path):
     k = np.array([[1.256637061435917236e-03, 2.5e-3]])
     c = np.array([[1.0, 2.0]])

@@ -119,3 +119,37 @@ def test_device_entry_point(cuda_device):
     torch.cuda.synchronize()
     assert np.array_equal(d_k.cpu().numpy().reshape(lmax, nmax), host.k_ln)
     assert np.array_equal(d_c.cpu().numpy().reshape(lmax, nmax), host.c_ln)
+
+
+@pytest.mark.parametrize("n,lmax,nmax,weighted", [
+    (1500, 12, 20, False),
+    (2500, 40, 70, True),     # 64-wide tiles in m and n, ragged
+    (3000, 256, 128, True),   # the split form's headline shape: l up to 255, z up to ~670
+])
+def test_poly_jl_vs_oracle_exact(cuda_device, n, lmax, nmax, weighted):
+    """CATANA_JL_POLY (piecewise FP64 polynomials, degree 11 per unit interval of
+    z = k r) against the oracle with exact j_l on the same points: the same 1e-10 bar
+    as the drop-in.  This mode is the FP64 reference the split form is measured
+    against at full catalog sizes (the exact branch costs O(l) per j_l)."""
+    pts = uniform_ball(n, 1000.0, seed=31 + n)
+    w = np.random.default_rng(n).uniform(0.5, 1.5, n) if weighted else None
+    res = catana.sfb_decomposition(catana.PointContainer(pts), lmax, nmax, 1000.0, True, False, weights=w,
+                                   interpolation="poly")
+    k, c, f = O.sfb_raw(pts, lmax, nmax, 1000.0, interpolated=False, weights=w)
+    fmax = max(np.abs(x).max() for x in f)
+    err = max(np.abs(a - b).max() for a, b in zip(res.f_lmn, f)) / fmax
+    print("poly n=%d lmax=%d nmax=%d: max|df|/max|f| = %.2e" % (n, lmax, nmax, err))
+    _compare(res, k, c, f)
+
+
+def test_poly_jl_radius_beyond_rmax_and_domain(cuda_device):
+    """The polynomial table is sized from the catalog's largest radius, so radii past
+    rmax are fine (unlike the lerp table); a negative radius is a ValueError."""
+    pts = uniform_ball(1200, 100.0, seed=4)
+    pts[17, 0] = 400.0
+    res = catana.sfb_decomposition(catana.PointContainer(pts), 6, 6, 100.0, True, False, interpolation="poly")
+    k, c, f = O.sfb_raw(pts, 6, 6, 100.0, interpolated=False)
+    _compare(res, k, c, f)
+    pts[3, 0] = -1.0
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition(catana.PointContainer(pts), 6, 6, 100.0, False, False, interpolation="poly")
