@@ -13,8 +13,9 @@ e2e     the same through the host-buffer C ABI (catana_gpu_sfb_raw): pinned host
 roofline  the dominant kernel (the tcgen05 contraction, k_split_l) timed with CUDA
         events inside the timed region; algorithmic work = 4 flops per point-mode;
         peak = measured dense bf16/fp16 burst peak / 3 (three hi/lo products per MAC).
-cpu_baseline  the oracle's OpenMP restatement of the reference's raw path on a
-        bounded point sample, all host cores, same lmax/nmax.
+cpu_baseline  the oracle's OpenMP restatement of the reference's raw path, all host
+        cores, same lmax/nmax: timed on samples of 300 and 1500 points, fitted as
+        fixed (the per-l j_l tables) + per-point cost, extrapolated to the catalog.
 
 --impl reference times only that CPU path (rank 0), a bounded sample per step.
 Multi-GPU (torchrun): every rank decomposes its own 10M-point shard of one catalog
@@ -50,7 +51,6 @@ def parse():
     p.add_argument("--nmax", type=int, default=128)
     p.add_argument("--rmax", type=float, default=1000.0)
     p.add_argument("--seed", type=int, default=2)
-    p.add_argument("--cpu-sample", type=int, default=600, help="points in the CPU baseline sample")
     p.add_argument("--plain-sample", type=int, default=20_000, help="points for the FP64 plain GPU comparison")
     p.add_argument("--side", type=int, default=1, help="also time the FP64 (100k, 32, 32) and HEALPix cases")
     p.add_argument("--no-extras", action="store_true", help="skip e2e/cpu/plain/accuracy legs")
@@ -135,31 +135,52 @@ def peaks():
         return 1900.0, 1700.0, 6800.0, "fallback"
 
 
-def cpu_baseline(pts, w, lmax, nmax, rmax):
-    """The oracle's restatement of sfb_raw.cpp on a bounded sample, all host cores."""
+def cpu_time(pts, w, lmax, nmax, rmax):
+    """Seconds of the oracle's OpenMP restatement of sfb_raw.cpp (per l: the lerp table,
+    then OpenMP over the points) on one point sample, all host cores."""
     from oracle import oracle as O
     O.build()
     t = time.perf_counter()
     O.sfb_raw(pts, lmax, nmax, rmax, interpolated=True, weights=w, store_flmn=False)
-    dt = time.perf_counter() - t
-    return pts.shape[0] * modes(lmax, nmax) / dt, dt
+    return time.perf_counter() - t
+
+
+def cpu_fit(a, n_small=300, n_large=1500):
+    """The CPU cost of the full catalog as fixed + per-point: each l rebuilds a
+    1000 nmax-node j_l table whatever the sample size (sfb_raw.cpp:45-49), so two
+    sample sizes separate that fixed cost from the per-point work, which is exactly
+    linear in N.  Returns (seconds for the full catalog, fixed s, s per point, note)."""
+    pts, w = catalog(n_large, a.rmax, a.seed)
+    cpu_time(pts[:50], w[:50], a.lmax, a.nmax, a.rmax)  # page in the library and OpenMP pool
+    ts = cpu_time(pts[:n_small], w[:n_small], a.lmax, a.nmax, a.rmax)
+    tl = cpu_time(pts, w, a.lmax, a.nmax, a.rmax)
+    slope = max(tl - ts, 1e-9) / (n_large - n_small)
+    fixed = max(0.0, tl - slope * n_large)
+    note = ("samples of %d and %d points of the same catalog (same lmax/nmax/rmax/weights, interpolated j_l as the "
+            "reference uses for N > 1000): %.2f s and %.2f s -> %.2f s fixed (per-l j_l tables) + %.3g s per point, "
+            "extrapolated to %d points" % (n_small, n_large, ts, tl, fixed, slope, a.points))
+    return fixed + slope * a.points, fixed, slope, note
 
 
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pts, w = catalog(a.cpu_sample, a.rmax, a.seed)
+    n_large = 1500
+    t_full, fixed, slope, note = cpu_fit(a, n_large=n_large)
+    pts, w = catalog(n_large, a.rmax, a.seed)
     for _ in range(a.warmup):
-        cpu_baseline(pts, w, a.lmax, a.nmax, a.rmax)
+        cpu_time(pts, w, a.lmax, a.nmax, a.rmax)
     t = time.perf_counter()
     for _ in range(a.steps):
-        cpu_baseline(pts, w, a.lmax, a.nmax, a.rmax)
+        cpu_time(pts, w, a.lmax, a.nmax, a.rmax)
     dt = (time.perf_counter() - t) / a.steps
-    v = a.cpu_sample * modes(a.lmax, a.nmax) / dt
+    # each step: the 1500-point sample; its per-point share after the fixed cost,
+    # extrapolated to the whole catalog
+    per_point = max(dt - fixed, 1e-9) / n_large
+    v = a.points * modes(a.lmax, a.nmax) / (fixed + per_point * a.points)
     cores = os.cpu_count()
-    sample = "%d of the %d points per step (same lmax/nmax/rmax/weights; the path is linear in N)" % (
-        a.cpu_sample, a.points)
+    sample = "each step %d of the %d points; fixed %.2f s from a calibration (%s)" % (n_large, a.points, fixed, note)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -776,14 +797,15 @@ def main():
             if a.stream_chunks > 0:
                 out["side"]["streamed_survey_l512_n256_split"] = streamed_workload(torch, _lib, catana,
                                                                                   chunks=a.stream_chunks)
-        # ---- CPU baseline: the oracle's OpenMP restatement on a bounded sample ----
-        cs = min(a.cpu_sample, a.points)
-        v, dt = cpu_baseline(np.ascontiguousarray(pts[:cs]), np.ascontiguousarray(w[:cs]), L, M, a.rmax)
+        # ---- CPU baseline: the oracle's OpenMP restatement, fixed + per-point fit ----
+        t_full, _, _, note = cpu_fit(a)
+        v = a.points * nmodes / t_full
         if a.side:
             out["side"]["next_rows"]["shot_noise_integrals_l32_n32"]["cpu_baseline"] = cpu_integrals_baseline()
             try:  # the FP64 drop-in case in full: 100k points, lmax = nmax = 32, unit weights, seed 0
                 p1, _ = catalog(100000, 1000.0, 0)
-                v1, t1 = cpu_baseline(p1, None, 32, 32, 1000.0)
+                t1 = cpu_time(p1, None, 32, 32, 1000.0)
+                v1 = 100000 * modes(32, 32) / t1
                 out["side"]["plain_fp64_100k_l32_n32"]["cpu_baseline"] = {
                     "value": v1, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                     "sample": "the whole workload (100k points), interpolated j_l as the reference uses for "
@@ -794,9 +816,7 @@ def main():
                 out["side"]["healpix_nside256_1M_l128_n64"]["cpu_baseline"] = cpu_healpix_baseline()
             except Exception as ex:  # a side measurement: never costs the main line
                 out["side"]["healpix_nside256_1M_l128_n64"]["cpu_baseline"] = {"error": repr(ex)}
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                               "sample": "%d points (of %d), same lmax/nmax/rmax/weights, interpolated j_l as the "
-                                         "reference uses for N > 1000; %.1f s" % (cs, a.points, dt)}
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": note}
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:

@@ -78,6 +78,7 @@ SIGNATURES = {
     "catana_gpu_sbessel_integrals": (ctypes.c_int, [_P, _I64, _D, _D, _U32, _D, _P, _P, _I64, _P, _P]),
     "catana_gpu_last_error": (ctypes.c_char_p, []),
     "catana_gpu_fp64_peak": (ctypes.c_int, [ctypes.c_int32, _P]),
+    "catana_gpu_test_split_stall": (ctypes.c_int, [_U32]),
     "catana_gpu_profile_enable": (None, [ctypes.c_int]),
     "catana_gpu_profile_report": (ctypes.c_int, [_P, _P, _P]),
     "catana_gpu_launch_count": (ctypes.c_uint64, []),

@@ -604,6 +604,10 @@ catana_status_t catana_gpu_sfb_raw(const double *points, const double *weights, 
         set_error("argument (z) outside of defined range.");
         return CATANA_ERR_DOMAIN;
     }
+    if (err_h != 0) {
+        set_error("split kernel reported a timed-out wait");
+        return CATANA_ERR_CUDA;
+    }
     return CATANA_OK;
 }
 

@@ -32,12 +32,12 @@
 //     representable (enough for lmax <= 256); the m = 0 step is rounded once
 //     (step_once), so Y_l0 carries no mean error over the sphere through which a
 //     catalog's monopole could leak into l > 0;
-//   * the seeds of every m column stay FP64: a per-point FP64 sectoral value P_ll
-//     (double-buffered by the parity of l) advances by P_ll = a_l s P_{l-1,l-1} in
-//     FP64 each level, and both P_ll and P_{l,l-1} = sqrt(2l+1) x P_{l-1,l-1} are
-//     formed from it in FP64 and rounded once into the FP32 rows -- so the FP32
-//     recurrence of column m starts from correctly rounded values at l = m, m + 1
-//     instead of inheriting m rounded sectoral steps;
+//   * the sectoral seeds stay FP64: before the level loop, k_split_sectoral advances
+//     every point's P_ll = -sqrt((2l+1)/(2l)) s P_{l-1,l-1} in FP64 from the FP32
+//     value of P_00 and stores each level's P_ll, rounded once, in slot m = l of the
+//     P_{l-1} row set -- a slot no level uses before level l reads it, and one the
+//     TMA staging of P_{l-1} already covers -- so column m of the FP32 recurrence
+//     starts from a correctly rounded P_mm instead of m rounded FP32 steps;
 //   * e^{-i m phi}: one sincospif of the exact phase (64-bit fixed-point fraction of a
 //     turn) per warp-run of <= 8 m, then complex rotation by e^{i phi}.
 // Pipeline: two operand buffers and two row stages.  Warps 0..15 generate the operands
@@ -54,6 +54,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -81,7 +82,7 @@ constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 
 constexpr int SPLIT_LMAX_EXT = 512; // with the 2-bit row exponents (extended range)
 constexpr int SPLIT_NMAX = 256;     // two 128-lane halves (separate work items)
 constexpr int NHALF = 128;          // radial orders per work item (accumulator lanes)
-constexpr uint64_t WAIT_NS = 1000000000ull;
+constexpr uint64_t WAIT_NS = 1000000000ull;  // drains of in-flight copies and MMAs before exit (1 s)
 
 // shared-memory map (bytes, from a 1024-aligned base)
 constexpr uint32_t SM_J = 8192;          // J hi or J lo: 4 k-groups x 2 atoms
@@ -101,7 +102,6 @@ constexpr uint32_t OFF_COEF = OFF_INV + NHALF * 4;      // recurrence coefficien
 constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
-constexpr double P00_SCALED_D = 0.28209479177387814347 * 1.2676506002282294e30;
 // Y operand = P * 2^12: the stored rows carry 2^100, so the readout factor is 2^-88.
 // Scaling both operands towards the top of the FP16 range keeps the lo halves normal.
 constexpr float Y_UNSCALE = 3.2311742677852644e-27f;  // 2^-88
@@ -131,7 +131,6 @@ struct SplitCat {
     const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..2, then exponent words of sets 0..2
     const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
-    double *sect;           // FP64 sectoral P_ll 2^100 per point, two sets [l & 1][stride]
 };
 
 // One CTA of a level launch: a catalog, a block of complex m, a range of tiles.
@@ -142,13 +141,14 @@ struct SplitItem {
 
 struct SplitArgs {
     int l, nint;
-    double a_sect, a_sub;    // FP64 seed coefficients of l: -sqrt((2l+1)/(2l)), sqrt(2l+1)
     const SplitItem *items;  // this level's items (one per CTA)
     const SplitCat *cats;
     const float4 *coef;      // recurrence coefficients, row l
     const float4 *tab;       // j_l table, row l: nint intervals x 2 float4
     float *partial;          // [item][256][128]
     int *err;
+    uint64_t wait_ns;        // limit of every pipeline wait (1 s; a test hook shortens it)
+    int stall;               // test hook: withhold the first operand hand-off of every item
 };
 
 __device__ __forceinline__ void store_split8(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, const float (&v)[8]) {
@@ -362,8 +362,6 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
     const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
     float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
-    const double *__restrict__ sect_prev = cat.sect + (size_t)((l + 1) & 1) * stride;  // FP64 P_{l-1,l-1}
-    double *__restrict__ sect_cur = cat.sect + (size_t)(l & 1) * stride;               // FP64 P_ll
     const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
     unsigned long long *ex0 = nullptr;
     if (EXT) {
@@ -380,11 +378,11 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     int folds = 0;
     bool ok = true;
 
-    auto wait_buf = [&](int b) -> bool {
+    auto wait_buf = [&](int b, uint64_t limit) -> bool {
         uint32_t &wt = b ? waited1 : waited0;
         const uint32_t us = b ? uses1 : uses0;
         while (wt < us) {
-            if (!tc05::mbar_wait(&mbar[b], wt & 1, WAIT_NS)) return false;
+            if (!tc05::mbar_wait(&mbar[b], wt & 1, limit)) return false;
             ++wt;
         }
         return true;
@@ -427,9 +425,9 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
         }
     };
-    auto wait_stage = [&](int sidx) -> bool {
+    auto wait_stage = [&](int sidx, uint64_t limit) -> bool {
         uint32_t &sw = sidx ? swait1 : swait0;
-        if (!tc05::mbar_wait(&sbar[sidx], sw & 1u, WAIT_NS)) return false;
+        if (!tc05::mbar_wait(&sbar[sidx], sw & 1u, limit)) return false;
         ++sw;
         return true;
     };
@@ -514,7 +512,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             bool okp = true;
             if (tid == 0 && t > t0 && t + 1 < t1) {  // stage (t+1)&1 last held tile t-1
                 uint32_t &gw = ((t + 1) & 1) ? gw1 : gw0;
-                okp = tc05::mbar_wait(&gfree[(t + 1) & 1], gw & 1, WAIT_NS);
+                okp = tc05::mbar_wait(&gfree[(t + 1) & 1], gw & 1, a.wait_ns);
                 ++gw;
             }
             if (!okp) {
@@ -523,7 +521,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 break;
             }
             prefetch_rows(t + 1);
-            if (!(wait_buf(b) && wait_stage((int)(t & 1)))) {
+            if (!(wait_buf(b, a.wait_ns) && wait_stage((int)(t & 1), a.wait_ns))) {
                 *abort_v = 1;
                 ok = false;
                 break;
@@ -708,35 +706,21 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                     if (mlh < mhi) {  // warp-uniform
                                         if (l == 0) {
                                             Pq = P00_SCALED;
-                                            if (wrows) sect_cur[i] = P00_SCALED_D;
-                                        } else if (mh >= l - 1) {
-                                            // FP64 seeds: P_ll = a_sect s P_{l-1,l-1} and
-                                            // P_{l,l-1} = a_sub x P_{l-1,l-1} from the per-point
-                                            // FP64 sectoral value, rounded once into the row
-                                            const bool sect = (mh == l);
-                                            const double pp = sect_prev[i];
-                                            double v = sect ? a.a_sect * ((double)sh + (double)sl) * pp
-                                                            : a.a_sub * ((double)xh + (double)xl) * pp;
-                                            if (sect && wrows) sect_cur[i] = v;
-                                            if (EXT) {  // the frame of P_{l-1,l-1}: stored value P 2^100 2^(128 e)
-                                                e = ebits(stge1[sect ? mlh - 1 : mlh], q);
-                                                for (unsigned k = 0; k < e; ++k) v *= 0x1p128;
-                                                Pq = (float)v;
-                                                if (sect) {
-                                                    if (fabsf(Pq) < 0x1p-40f) {
-                                                        if (e < 3) {
-                                                            Pq = (float)(v * 0x1p128);
-                                                            ++e;
-                                                        } else {
-                                                            Pq = 0.f;  // below 2^-520: no contribution within lmax
-                                                        }
-                                                    }
-                                                } else if (e > 0 && fabsf(Pq) > 0x1p40f) {
-                                                    Pq = (float)(v * 0x1p-128);
-                                                    --e;
-                                                }
-                                            } else {
-                                                Pq = (float)v;
+                                        } else if (mh == l) {
+                                            // the FP64 sectoral seed, rounded once by k_split_sectoral
+                                            // into slot l of the P_{l-1} set (EXT: with its exponent)
+                                            Pq = stg1[mlh * KT + q];
+                                            if (EXT) e = ebits(stge1[mlh], q);
+                                        } else if (mh == l - 1) {
+                                            // P_{l,l-1} = sqrt(2l+1) x P_{l-1,l-1}, rounded once
+                                            const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
+                                            const float p1 = stg1[mlh * KT + q];
+                                            if (EXT) e = ebits(stge1[mlh], q);
+                                            const float tt = fmaf(xh, p1, xl * p1);
+                                            Pq = step_once(A_hi, A_lo, 0.f, 0.f, tt, 0.f);
+                                            if (EXT && e > 0 && fabsf(Pq) > 0x1p40f) {
+                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                --e;
                                             }
                                         } else {  // m <= l - 2: one recurrence step, rounded once
                                             const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
@@ -785,22 +769,22 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             }
             tc05::fence_proxy_async();
             ws_arrive(&gfree[t & 1]);
-            ws_arrive(&fbar[b]);
+            if (!(a.stall && t == t0)) ws_arrive(&fbar[b]);  // the test hook withholds the first hand-off
             if (b) ++uses1; else ++uses0;
         }
         // stage loads still in flight (a loop that stopped early) land before the CTA exits
-        while (swait0 < sfill0 && wait_stage(0)) {
+        while (swait0 < sfill0 && wait_stage(0, WAIT_NS)) {
         }
-        while (swait1 < sfill1 && wait_stage(1)) {
+        while (swait1 < sfill1 && wait_stage(1, WAIT_NS)) {
         }
     } else {
         uint32_t fw0 = 0, fw1 = 0;  // fbar phases waited
         for (int64_t t = t0; t < t1; ++t) {
             const int b = (int)((t - t0) & 1);
             uint32_t &fw = b ? fw1 : fw0;
-            bool okw = tc05::mbar_wait(&fbar[b], fw & 1, WAIT_NS);
+            bool okw = tc05::mbar_wait(&fbar[b], fw & 1, a.wait_ns);
             ++fw;
-            if (okw && t > t0) okw = wait_buf(b ^ 1);  // the MMAs of tile t-1 (D_tile) complete
+            if (okw && t > t0) okw = wait_buf(b ^ 1, a.wait_ns);  // the MMAs of tile t-1 (D_tile) complete
             if (!fold_vote(okw && !*abort_v)) {        // the fold warps decide together
                 *abort_v = 1;
                 ok = false;
@@ -835,17 +819,18 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         }
         if (ok && t1 > t0) {
             const int lb = (int)((t1 - 1 - t0) & 1);
-            ok = fold_vote(wait_buf(lb));
+            ok = fold_vote(wait_buf(lb, a.wait_ns));
             if (ok) {
                 fold();
                 flush();
             }
         }
-        if (ok) ok = fold_vote(wait_buf(0) && wait_buf(1));
+        if (ok) ok = fold_vote(wait_buf(0, a.wait_ns) && wait_buf(1, a.wait_ns));
         if (!ok) {
-            // give in-flight MMAs a last bounded chance to land before TMEM is released
-            wait_buf(0);
-            wait_buf(1);
+            // MMAs already issued land before TMEM is released (bounded by the 1 s
+            // drain limit, not by the possibly shortened pipeline limit)
+            wait_buf(0, WAIT_NS);
+            wait_buf(1, WAIT_NS);
             *abort_v = 1;
         }
     }
@@ -858,6 +843,49 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     __syncthreads();
     tc05::fence_after();
     if (warp == 0) tc05::tmem_dealloc(tmem, tcols);
+}
+
+// Sectoral seeds (one warp per tile, lane = point): P_ll 2^100 advanced in FP64,
+// P_ll = a_l s P_{l-1,l-1} from the FP32 value of P_00 (the row every m = 0 step
+// uses, so the m = 0 recurrence sees one consistent P_00), rounded once and stored in
+// slot m = l of the P_{l-1} row set for l = 1 .. lmax-1.  Extended range: in the
+// frame of the running 2-bit exponent (stored value P 2^100 2^(128 e), e raised when
+// the value drops below 2^-40, 0 below 2^-520), with the exponent word written too.
+__global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const double *__restrict__ asect,
+                                 int64_t ntiles, int ext) {
+    const SplitCat c = cats[cat];
+    const int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= ntiles) return;  // warp-uniform
+    const int q = threadIdx.x & 31;
+    const int64_t i = t * KT + q;
+    const SplitPt &pt = c.pts[i];
+    const double s = (double)pt.s_hi + (double)pt.s_lo;
+    const size_t set = (size_t)c.stride * c.lrows;
+    double P = (double)P00_SCALED;
+    unsigned e = 0;
+    for (int l = 1; l < lmax; ++l) {
+        P = asect[l] * s * P;
+        const int k = (l + 2) % 3;  // the set of P_{l-1}
+        float v;
+        if (ext) {
+            double f = P;
+            for (unsigned j = 0; j < e; ++j) f *= 0x1p128;
+            v = (float)f;
+            if (fabsf(v) < 0x1p-40f) {
+                if (e < 3) {
+                    ++e;
+                    v = (float)(f * 0x1p128);
+                } else {
+                    v = 0.f;  // below 2^-520: no contribution within lmax
+                }
+            }
+            const unsigned b0 = __ballot_sync(0xffffffffu, e & 1u), b1 = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
+            if (q == 0) c.rexp[(size_t)k * c.eset + t * c.epitch + l] = ((unsigned long long)b1 << 32) | b0;
+        } else {
+            v = (float)P;
+        }
+        c.rows[(size_t)k * set + (size_t)l * c.stride + i] = v;
+    }
 }
 
 // One catalog's reduction at one level: its items are ordered block-major, then slab.
@@ -1166,6 +1194,8 @@ std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
 
 }  // namespace
 
+std::atomic<uint64_t> g_split_stall_ns{0};
+
 catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_in, bool use_graph,
                           double waves, int *err_dev, cudaStream_t st) {
     std::vector<CatPlan> cats;
@@ -1184,6 +1214,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         cats.push_back(p);
     }
     if (cats.empty()) return CATANA_OK;
+    // the test hook (catana_gpu_test_split_stall) arms one run
+    const uint64_t stall_ns = g_split_stall_ns.exchange(0);
     if (!ctx->attr_split) {
         CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SMEM_BYTES));
@@ -1291,7 +1323,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
         size_t ws_bytes = 0;
-        std::vector<size_t> off_pts(gn), off_rows(gn), off_exp(gn), off_sect(gn);
+        std::vector<size_t> off_pts(gn), off_rows(gn), off_exp(gn);
         for (int c = c0; c < c1; ++c) smax = std::max(smax, cats[c].stride);
         const size_t keyb = al256((size_t)smax * 4), histb = al256((size_t)256 * ((smax + 4095) / 4096 + 1) * 4);
         ws_bytes = 4 * keyb + histb;
@@ -1302,8 +1334,6 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             ws_bytes += al256((size_t)3 * cats[c].stride * cats[c].in.lmax * sizeof(float));
             off_exp[c - c0] = ws_bytes;
             if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
-            off_sect[c - c0] = ws_bytes;
-            ws_bytes += al256((size_t)2 * cats[c].stride * sizeof(double));
         }
         CG_CUDA_TRY(ctx->split_ws.ensure(ws_bytes));
         char *ws = ctx->split_ws.as<char>();
@@ -1394,6 +1424,10 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             o_kz[c - c0] = put(kz.data(), kz.size() * sizeof(float4));
             o_nl[c - c0] = put(P.nmax_l.data(), P.nmax_l.size() * sizeof(int));
         }
+        // FP64 coefficients of the sectoral step, -sqrt((2l+1)/(2l)) for l < lmax_g
+        std::vector<double> asect(lmax_g + 1, 0.0);
+        for (int l = 1; l < lmax_g; ++l) asect[l] = -std::sqrt((2.0 * l + 1.0) / (2.0 * l));
+        const size_t o_as = put(asect.data(), asect.size() * sizeof(double));
         // catalog descriptors (fixed for the group)
         const size_t o_cats = al256(host.size());
         host.resize(o_cats + (size_t)gn * sizeof(SplitCat));
@@ -1413,7 +1447,6 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.tmaps = nullptr;  // patched at upload
             sc.kz = nullptr;  // patched below, once the plan buffer's address is known
             sc.nmax_l = nullptr;
-            sc.sect = reinterpret_cast<double *>(ws + off_sect[c - c0]);
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
         // Work items of every level for a schedule of `waves` CTAs per SM: at level l
@@ -1534,14 +1567,14 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             SplitArgs a;
             a.l = l;
             a.nint = nint_tab;
-            a.a_sect = l >= 1 ? -std::sqrt((2.0 * l + 1.0) / (2.0 * l)) : 0.0;
-            a.a_sub = std::sqrt(2.0 * l + 1.0);
             a.items = reinterpret_cast<const SplitItem *>(pd + o_items) + S.item0[l];
             a.cats = reinterpret_cast<const SplitCat *>(pd + o_cats);
             a.coef = coef_d + (size_t)l * (l + 1) / 2;
             a.tab = tab + (size_t)l * nint_tab * 2;
             a.partial = ctx->partial.as<float>();
             a.err = err_dev;
+            a.wait_ns = stall_ns ? stall_ns : WAIT_NS;
+            a.stall = stall_ns ? 1 : 0;
             return a;
         };
 
@@ -1596,6 +1629,20 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         s = upload(S);
         if (s != CATANA_OK) return s;
         float *partial = ctx->partial.as<float>();
+        // ---- FP64 sectoral seeds of every level, after the autotuner's trial launches
+        // (which write rows) and before the level loop ----
+        {
+            for (int c = c0; c < c1; ++c) {
+                const int64_t nt = cats[c].ntiles;
+                if (cats[c].in.lmax < 2 || nt == 0) continue;
+                k_split_sectoral<<<ceil_div(nt, 8), 256, 0, st>>>(reinterpret_cast<const SplitCat *>(pd + o_cats),
+                                                                  c - c0, cats[c].in.lmax,
+                                                                  reinterpret_cast<const double *>(pd + o_as), nt,
+                                                                  ext ? 1 : 0);
+                count_launch();
+            }
+            CG_CUDA_TRY(cudaGetLastError());
+        }
         // ---- the level loop (optionally captured as one CUDA graph) ----
         auto levels = [&](bool profile, cudaStream_t ls_st) -> catana_status_t {
             for (int l = 0; l < lmax_g; ++l) {
@@ -1669,3 +1716,12 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
 }
 
 }  // namespace catana_gpu
+
+extern "C" catana_status_t catana_gpu_test_split_stall(uint32_t wait_us) {
+    if (wait_us == 0 || wait_us > 1000000u) {
+        catana_gpu::set_error("test_split_stall: wait_us must be in [1, 1000000]");
+        return CATANA_ERR_ARG;
+    }
+    catana_gpu::g_split_stall_ns.store((uint64_t)wait_us * 1000ull);
+    return CATANA_OK;
+}

@@ -321,6 +321,15 @@ catana_status_t catana_gpu_profile_report(double *kernel_ms, uint64_t *launches,
  * the plain path's roofline.  No counterpart in the reference. */
 catana_status_t catana_gpu_fp64_peak(int32_t ms, double *tflops);
 
+/* Test hook for the split kernel's bounded waits (no counterpart in the reference,
+ * whose GSL errors are switched off, sfb_raw.cpp:26).  Arms the next split-form run
+ * only: every work item withholds the hand-off of its first tile's operands, so the
+ * tensor-core warps' wait on it -- limited to wait_us microseconds for that run
+ * instead of 1 s -- runs out.  The kernel then stops issuing work, lets copies and
+ * MMAs already in flight land, frees its tensor memory and records CATANA_ERR_CUDA,
+ * which the entry point returns; the context stays usable.  wait_us in [1, 1e6]. */
+catana_status_t catana_gpu_test_split_stall(uint32_t wait_us);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char *catana_gpu_last_error(void);
 

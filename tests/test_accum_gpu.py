@@ -98,3 +98,48 @@ def test_accum_errors(cuda_device):
     with catana.SFBAccumulator(4, 4, 10.0, precision="plain") as acc2:
         with pytest.raises(ValueError):
             acc2.add(bad)
+
+
+def _survey(n, seed, rmax=1500.0, a=300.0):
+    """float32 (r, theta, phi): radial pdf ~ r^2 exp(-(r/a)^2) cut at rmax, the band
+    |theta - pi/2| < 20 deg masked out, phi uniform (the streamed survey's shape)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    smin = np.sin(np.deg2rad(20.0))
+    while sum(len(x) for x in out) < n:
+        r = a / np.sqrt(2.0) * np.sqrt((rng.standard_normal((n, 3)) ** 2).sum(1))
+        r = r[r < rmax]
+        ct = rng.uniform(smin, 1.0, r.size) * np.where(rng.random(r.size) < 0.5, -1.0, 1.0)
+        out.append(np.stack([r, np.arccos(ct), rng.uniform(0.0, 2.0 * np.pi, r.size)], 1))
+    return np.concatenate(out)[:n].astype(np.float32)
+
+
+def test_accum_13_chunks_matches_one_shot(sm103):
+    """The streamed survey's chunk count: 13 float32 chunks from pinned host memory
+    (copies of chunk k+1 overlapping the decomposition of chunk k) give the one-shot
+    split result of the whole catalog, and the split error measures against the FP64
+    plain path (polynomial j_l) on the same float32 values."""
+    torch = pytest.importorskip("torch")
+    n, k = 26000, 13
+    pts32 = _survey(n, seed=65)
+    pinned = [torch.from_numpy(np.ascontiguousarray(c)).pin_memory() for c in _chunks(pts32, k)]
+    lmax, nmax = 96, 64
+    with catana.SFBAccumulator(lmax, nmax, 1500.0, precision="split") as acc:
+        for c in pinned:
+            acc.add(c.numpy())
+        r = acc.finish(store_flmn=True)
+    pts64 = pts32.astype(np.float64)
+    one = catana.sfb_decomposition(catana.PointContainer(pts64), lmax, nmax, 1500.0, True, False, precision="split")
+    fmax = max(np.abs(x).max() for x in one.f_lmn)
+    assert max(np.abs(a - b).max() for a, b in zip(r.f_lmn, one.f_lmn)) <= 2e-6 * fmax
+    rp = catana.sfb_decomposition(catana.PointContainer(pts64), lmax, nmax, 1500.0, True, False, interpolation="poly")
+    fmax = max(np.abs(x).max() for x in rp.f_lmn)
+    assert max(np.abs(a - b).max() for a, b in zip(r.f_lmn, rp.f_lmn)) <= 1e-5 * fmax
+    # the radial profile leaves some (l, n) with j_l(k r) deep in its evanescent zone
+    # at every point: compare C_ln above 1e-30 of the largest (FP32 operand range)
+    keep = rp.c_ln >= 1e-30 * rp.c_ln.max()
+    rel = np.abs(r.c_ln - rp.c_ln)[keep] / rp.c_ln[keep]
+    print("accum split 13 chunks: C rel median %.2e p99 %.2e (%d of %d modes)" %
+          (np.median(rel), np.percentile(rel, 99), keep.sum(), keep.size))
+    assert keep.mean() > 0.9
+    assert np.median(rel) <= 5e-7 and np.percentile(rel, 99) <= 2e-6

@@ -47,6 +47,9 @@ def test_noalloc_matches_allocating_entry_twice(cuda_device):
     cases = [
         (uniform_ball(20000, 1000.0, seed=0), np.random.default_rng(0).uniform(0.5, 1.5, 20000), 32, 32, 1000.0),
         (uniform_ball(3000, 250.0, seed=1), None, 16, 20, 250.0),
+        # about 26k points fit the fixed array per chunk at lmax = nmax = 32: 60k points
+        # run the chunk loop three times (Legendre rows restarted, partials accumulated)
+        (uniform_ball(60000, 1000.0, seed=2), np.random.default_rng(2).uniform(0.5, 1.5, 60000), 32, 32, 1000.0),
     ]
     for pts, w, lmax, nmax, rmax in cases:
         k0, c0, f0 = _run("dev", pts, w, lmax, nmax, rmax, torch)
