@@ -99,7 +99,13 @@ constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;          // per n pair: (kz_hi, kz
 constexpr uint32_t OFF_JS = OFF_KZ + NHALF * 8;         // J scale 2^s_ln per n
 constexpr uint32_t OFF_INV = OFF_JS + NHALF * 4;        // readout 2^-s_ln 2^-12 per n
 constexpr uint32_t OFF_COEF = OFF_INV + NHALF * 4;      // recurrence coefficients, m pairs
-constexpr uint32_t SMEM_BYTES = OFF_COEF + MBLK * 16 + 1024;  // + alignment slack
+constexpr uint32_t OFF_JT = OFF_COEF + MBLK * 16;       // per operand warp: Taylor coefficients of its 8 J rows
+constexpr uint32_t SMEM_BYTES = OFF_JT + (NTHR / 32) * 32 * 4 + 1024;  // + alignment slack
+static_assert(SMEM_BYTES <= 232448, "k_split_l shared memory");
+// J of a tile comes from a cubic Taylor expansion about its record-16 radius when
+// k_max max|r - r_c| <= JT_TAU: the omitted terms are below JT_TAU^4 / 24 ~ 7e-9 of j_l's
+// envelope (the interpolant's derivatives are bounded by it)
+constexpr float JT_TAU = 0.02f;
 
 constexpr float P00_SCALED = 0.28209479177387814347f * 1.2676506002282294e30f;  // 1/sqrt(4 pi) * 2^100
 // Y operand = P * 2^12: the stored rows carry 2^100, so the readout factor is 2^-88.
@@ -112,7 +118,8 @@ struct SplitPt {
     float r_hi, r_lo, w;        // radius (float-float), weight
     float x_hi, x_lo;           // cos(theta) (float-float)
     float s_hi, s_lo;           // sin(theta) (float-float)
-    float cphi, sphi, pad;      // e^{i phi}
+    float cphi, sphi;           // e^{i phi}
+    float dr;                   // r - r of the tile's record 16; record 16 itself: max |dr| of the tile
     unsigned long long u;       // phi / 2pi as a 64-bit fraction of a turn
 };
 static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
@@ -305,6 +312,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     float *s_inv = reinterpret_cast<float *>(sm + OFF_INV);
     float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
+    const float kmax_j = nmax > 0 ? kz_row[nmax - 1].x : 0.f;  // largest k_ln / H of this half (k grows with n)
     for (int t = tid; t < 2 * a.nint; t += NTOT) s_tab[t] = a.tab[t];
     // radial orders past this half's count get k = 0 and J scale 0: their J rows are zero
     for (int t = tid; t < NHALF / 2; t += NTOT) {
@@ -542,6 +550,58 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const float2 w2 = make_float2(pt.w, pt.w);
                 const int n0 = 8 * g;
                 float2 v[4];
+                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                                                                       2 * SM_STROW + 16 * 48);
+                if (kmax_j * pc.dr <= JT_TAU) {  // the same for every thread of the CTA
+                    // J(n, q) = w_q sum_j c'_j dr_q^j about the tile's record-16 radius r_c:
+                    // c'_j = 2^s_n k_n^j p^(j)(u0_n) / j!, p the interval polynomial, u0_n the
+                    // offset of z_n = k_n r_c in its interval (float-float product)
+                    float *cs = reinterpret_cast<float *>(sm + OFF_JT) + 32 * g;
+                    __syncwarp();
+                    if (lane < 8) {
+                        const int n = n0 + lane;
+                        const float4 kk = s_kzp[n >> 1];
+                        const float kx = (n & 1) ? kk.y : kk.x, ky = (n & 1) ? kk.w : kk.z;
+                        const float p = __fmul_rn(pc.r_hi, kx);
+                        float e = fmaf(pc.r_hi, kx, -p);
+                        e = fmaf(pc.r_hi, ky, e);
+                        e = fmaf(pc.r_lo, kx, e);
+                        const float fl = rintf(p);
+                        const float u0 = __fadd_rn(__fadd_rn(p, -fl), e);
+                        const unsigned ia = min((unsigned)(int)fl, (unsigned)(a.nint - 1));
+                        const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                        // Taylor shift by synthetic division: b_0..b_3 = p(u0), p'(u0), p''(u0)/2, p'''(u0)/6
+                        float b0 = a0.x, b1 = a0.y, b2 = a0.z, b3 = a0.w, b4 = a1.x, b5 = a1.y;
+                        const float b6 = a1.z;
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2); b1 = fmaf(b2, u0, b1); b0 = fmaf(b1, u0, b0);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2); b1 = fmaf(b2, u0, b1);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        const float js = s_js[n];
+                        const float k1 = kx * js, k2 = k1 * kx, k3 = k2 * kx;
+                        // pair layout: (c0 n, c0 n+1, c1 n, c1 n+1, c2 n, c2 n+1, c3 n, c3 n+1)
+                        float *o = cs + 8 * (lane >> 1) + (lane & 1);
+                        o[0] = b0 * js;
+                        o[2] = b1 * k1;
+                        o[4] = b2 * k2;
+                        o[6] = b3 * k3;
+                    }
+                    __syncwarp();
+                    const float dq = (q == 16) ? 0.f : pt.dr;
+                    const float2 d2 = make_float2(dq, dq);
+    #pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float4 ca = *reinterpret_cast<const float4 *>(cs + 8 * k);
+                        const float4 cb = *reinterpret_cast<const float4 *>(cs + 8 * k + 4);
+                        float2 jv = __ffma2_rn(make_float2(cb.z, cb.w), d2, make_float2(cb.x, cb.y));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.z, ca.w));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.x, ca.y));
+                        v[k] = __fmul2_rn(jv, w2);
+                    }
+                } else {
     #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int n = n0 + 2 * k;
@@ -573,6 +633,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                     const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
                     v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
                 }
+                }
                 store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
             }
             else {
@@ -582,6 +643,59 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(pt.w, pt.w);
+                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                                                                       2 * SM_STROW + 16 * 48);
+                if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
+                    float *cs = reinterpret_cast<float *>(sm + OFF_JT) + 32 * g;
+                    __syncwarp();
+                    if (lane < 2 * (jp1 - jp0)) {  // rows past the count have k = 0, J scale 0: zero coefficients
+                        const int n = 2 * jp0 + lane;
+                        const float4 kk = s_kzp[n >> 1];
+                        const float kx = (n & 1) ? kk.y : kk.x, ky = (n & 1) ? kk.w : kk.z;
+                        const float p = __fmul_rn(pc.r_hi, kx);
+                        float e = fmaf(pc.r_hi, kx, -p);
+                        e = fmaf(pc.r_hi, ky, e);
+                        e = fmaf(pc.r_lo, kx, e);
+                        const float fl = rintf(p);
+                        const float u0 = __fadd_rn(__fadd_rn(p, -fl), e);
+                        const unsigned ia = min((unsigned)(int)fl, (unsigned)(a.nint - 1));
+                        const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                        float b0 = a0.x, b1 = a0.y, b2 = a0.z, b3 = a0.w, b4 = a1.x, b5 = a1.y;
+                        const float b6 = a1.z;
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2); b1 = fmaf(b2, u0, b1); b0 = fmaf(b1, u0, b0);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2); b1 = fmaf(b2, u0, b1);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        b2 = fmaf(b3, u0, b2);
+                        b5 = fmaf(b6, u0, b5); b4 = fmaf(b5, u0, b4); b3 = fmaf(b4, u0, b3);
+                        const float js = s_js[n];
+                        const float k1 = kx * js, k2 = k1 * kx, k3 = k2 * kx;
+                        float *o = cs + 8 * (lane >> 1) + (lane & 1);
+                        o[0] = b0 * js;
+                        o[2] = b1 * k1;
+                        o[4] = b2 * k2;
+                        o[6] = b3 * k3;
+                    }
+                    __syncwarp();
+                    const float dq = (q == 16) ? 0.f : pt.dr;
+                    const float2 d2 = make_float2(dq, dq);
+                    for (int jp = jp0; jp < jp1; ++jp) {
+                        const float *c8 = cs + 8 * (jp - jp0);
+                        const float4 ca = *reinterpret_cast<const float4 *>(c8);
+                        const float4 cb = *reinterpret_cast<const float4 *>(c8 + 4);
+                        float2 jv = __ffma2_rn(make_float2(cb.z, cb.w), d2, make_float2(cb.x, cb.y));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.z, ca.w));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.x, ca.y));
+                        const float2 v = __fmul2_rn(jv, w2);
+                        __half2 hh = __float22half2_rn(v);
+                        const float2 hf = __half22float2(hh);
+                        __half2 ll = __float22half2_rn(__fadd2_rn(v, make_float2(-hf.x, -hf.y)));
+                        const uint32_t off = tc05::mn_sw128_off(2 * jp, q, 2);
+                        *reinterpret_cast<__half2 *>(jhi + off) = hh;
+                        *reinterpret_cast<__half2 *>(jlo + off) = ll;
+                    }
+                } else
                 for (int jp = jp0; jp < jp1; ++jp) {
                     const int n = 2 * jp;
                     const float4 kk = s_kzp[jp];
@@ -803,16 +917,24 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             if (tid == NTHR) {
                 const uint32_t sj_hi = tc05::smem_u32(jhi), sj_lo = tc05::smem_u32(jlo);
                 const uint32_t sy_hi = tc05::smem_u32(yhi), sy_lo = tc05::smem_u32(ylo);
+                // the four small hi x lo / lo x hi products first, the two hi x hi last: the
+                // tensor core rounds each MMA's sum into the FP32 accumulator, and the
+                // small terms then round at their own magnitude (2^-11 of the sum), so
+                // only two roundings per tile fall at the full magnitude instead of five
+                uint64_t ah[2], al[2], bh[2], bl[2];
     #pragma unroll
                 for (int ks = 0; ks < 2; ++ks) {
-                    const uint64_t ah = tc05::desc_sw128(sj_hi + ks * 4096, 1024, 2048);
-                    const uint64_t al = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
-                    const uint64_t bh = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
-                    const uint64_t bl = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
-                    tc05::mma_f16(d_tile, ah, bh, idesc, (ks == 0 && fresh_tile) ? 0u : 1u);
-                    tc05::mma_f16(d_tile, ah, bl, idesc, 1u);
-                    tc05::mma_f16(d_tile, al, bh, idesc, 1u);
+                    ah[ks] = tc05::desc_sw128(sj_hi + ks * 4096, 1024, 2048);
+                    al[ks] = tc05::desc_sw128(sj_lo + ks * 4096, 1024, 2048);
+                    bh[ks] = tc05::desc_sw128(sy_hi + ks * 8192, 1024, 4096);
+                    bl[ks] = tc05::desc_sw128(sy_lo + ks * 8192, 1024, 4096);
                 }
+                tc05::mma_f16(d_tile, ah[0], bl[0], idesc, fresh_tile ? 0u : 1u);
+                tc05::mma_f16(d_tile, al[0], bh[0], idesc, 1u);
+                tc05::mma_f16(d_tile, ah[1], bl[1], idesc, 1u);
+                tc05::mma_f16(d_tile, al[1], bh[1], idesc, 1u);
+                tc05::mma_f16(d_tile, ah[0], bh[0], idesc, 1u);
+                tc05::mma_f16(d_tile, ah[1], bh[1], idesc, 1u);
                 tc05::commit(&mbar[b]);
             }
             if (b) ++uses1; else ++uses0;
@@ -921,14 +1043,24 @@ __global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const
 // Point preparation, in radius-sorted order: float-float r, cos(theta), sin(theta);
 // e^{i phi} in FP32; the 64-bit phase fraction; FP32 weights.  Flags radii that are
 // negative or not finite.  Records past n (padding to whole tiles) are zeroed.
+// Each record also carries dr = r - r_c, r_c the radius of its tile's record 16 (0 if
+// that record is padding), and record 16 carries the tile's max |dr| instead: the J
+// operand of a tile whose radii lie close together comes from a Taylor expansion
+// about r_c (k_split_l).  One warp per tile (blockDim a multiple of 32).
 template <typename T>
 __global__ void k_split_prep(const T *__restrict__ pts, const T *__restrict__ w,
                              const uint32_t *__restrict__ perm, int64_t n, int64_t npad, SplitPt *out, int *err) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= npad) return;
+    if (i - (threadIdx.x & 31) >= npad) return;  // whole warps (npad is a multiple of 32)
+    const int64_t ic = (i & ~(int64_t)31) + 16;
+    const double rc = ic < n ? (double)pts[3 * (int64_t)perm[ic]] : 0.0;
+    const double dr = i < n ? (double)pts[3 * (int64_t)perm[i]] - rc : 0.0;
+    float dmax = (float)fabs(dr);
+    for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     SplitPt o;
     if (i >= n) {
-        o.r_hi = o.r_lo = o.w = o.x_hi = o.x_lo = o.s_hi = o.s_lo = o.cphi = o.sphi = o.pad = 0.f;
+        o.r_hi = o.r_lo = o.w = o.x_hi = o.x_lo = o.s_hi = o.s_lo = o.cphi = o.sphi = 0.f;
+        o.dr = (threadIdx.x & 31) == 16 ? dmax : 0.f;
         o.u = 0ull;
         out[i] = o;
         return;
@@ -947,7 +1079,7 @@ __global__ void k_split_prep(const T *__restrict__ pts, const T *__restrict__ w,
     o.s_lo = (float)(st - (double)o.s_hi);
     o.cphi = (float)cp;
     o.sphi = (float)sp;
-    o.pad = 0.f;
+    o.dr = (threadIdx.x & 31) == 16 ? dmax : (float)dr;
     double f = ph * 0.15915494309189533577;  // phi / 2pi
     f -= floor(f);
     const double scaled = ldexp(f, 64);
