@@ -723,20 +723,22 @@ def main():
         kernel = "k_fp64_raw_l"
     achieved = (kfl.value / (kms.value / 1e3)) / 1e12 if kms.value > 0 else None
     # DRAM bytes of an average k_split_l launch: the ncu capture of l = 200 on 300k points
-    # (profiles/k_split_l_l200_300k_full.md) read+wrote 847 MB = 1.15 x the algorithmic
-    # 12 B per (point, m) of Legendre rows + 48 B per point (738 MB); scaled here to this
-    # run's chunk size and averaged over l.
+    # (profiles/k_split_l_l200_300k_full.md) read+wrote 753 MB = 1.02 x the algorithmic
+    # 12 B per (point, m) of Legendre rows + 48 B per point (738 MB); the traffic grows in
+    # proportion to points x (l + 1), so that ratio is applied here to this run's catalog
+    # pieces and averaged over the launches.
     traffic = None
     if a.form == "split":
         chunk = min(a.points, int(16e9 / (12.0 * L)))
         avg = sum((12.0 * (l + 1) + 48.0) * chunk for l in range(L)) / L
-        traffic = 1.15 * avg
+        traffic = 1.02 * avg
     if a.form == "split":
         peak_note = peak_note.replace("0.0 s step", "%.1f s step" % (ms_step / 1e3))
     roof = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
             "frac_of_burst_peak": (achieved / (bf16 / 3.0)) if (achieved and a.form == "split") else None,
-            "traffic_unit": "bytes per launch (average over l), from one ncu capture scaled by points",
+            "traffic_unit": "bytes per launch (average over l): one ncu capture (l = 200, 300k points) scaled "
+                            "by points x (l + 1)",
             "peak_source": peak_note,
             "kernel_ms_per_step": kms.value / a.steps, "kernel_launches_per_step": int(kn.value) // max(1, a.steps),
             "kernel_share_of_step": (kms.value / ms_total) if ms_total > 0 else None,
