@@ -127,10 +127,12 @@ static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 // One catalog (or catalog chunk) of a split-form plan.
 struct SplitCat {
     const SplitPt *pts;     // radius-sorted point records, padded to whole tiles
-    float *rows;            // three Legendre row sets; set k at rows + k * stride * lrows
+    float *rows;            // three Legendre row sets, tile-major with m pairs interleaved: value (m, point
+                            // 32 t + q) of set k at rows + k * stride * lrp + t * 32 lrp + 64 (m / 2) + 2 q + m % 2
     int64_t n;              // points
     int stride;             // row stride (multiple of 32, >= n)
     int lrows;              // rows per set (the catalog's lmax)
+    int lrp;                // lrows rounded up to even (m pairs per tile block: lrp / 2)
     int kzw;                // row width of kz (the catalog's nmax)
     int epitch;             // exponent words per tile (lrows rounded up to even)
     unsigned long long *rexp;  // extended range: three exponent sets [tile][lrows], set k at rexp + k * eset
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const int mlo = 2 * pb0, mhi = min(2 * pb1, mcount);  // local m range of this warp
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
-    const size_t set = (size_t)stride * cat.lrows;
+    const size_t set = (size_t)stride * cat.lrp;
     const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
     const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
     float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
@@ -424,10 +426,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         tc05::fence_proxy_async();  // earlier generic reads of this stage before the async writes
         tc05::mbar_arrive_expect_tx(&sbar[sidx], stage_bytes);
         tc05::bulk_g2s(stg + 2 * SM_STROW, cat.pts + t * KT, SM_STPTS, &sbar[sidx]);
-        const int x = (int)(t * KT);
-        for (int k = 0; k < nb1; ++k) tc05::tma_load_2d(stg + k * 4096, tm_r1, x, mb0 + 32 * k, &sbar[sidx]);
+        // 32 m (16 interleaved pairs) x 32 points per box: 4 KB contiguous in the tile-major rows
+        for (int k = 0; k < nb1; ++k) tc05::tma_load_3d(stg + k * 4096, tm_r1, 0, (mb0 >> 1) + 16 * k, (int)t, &sbar[sidx]);
         for (int k = 0; k < nb2; ++k)
-            tc05::tma_load_2d(stg + SM_STROW + k * 4096, tm_r2, x, mb0 + 32 * k, &sbar[sidx]);
+            tc05::tma_load_3d(stg + SM_STROW + k * 4096, tm_r2, 0, (mb0 >> 1) + 16 * k, (int)t, &sbar[sidx]);
         if (EXT && l > 0) {
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
@@ -743,7 +745,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 sma *= Y_UNSCALE;
                 float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
                 float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
-                float *rowp = st0 + (int64_t)(mb0 + mlo) * stride + i;  // P_l row of the pair's first m
+                // P_l of the pair (m, m + 1) at this point (m even: the pair is one float2)
+                float *rowp = st0 + (size_t)t * KT * cat.lrp + (size_t)(mb0 + mlo) * KT + 2 * q;
                 const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
                 const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
                 const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
@@ -758,8 +761,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                             if (m + 1 <= l - 2 && ml + 1 < mcount) {
                                 // both m take the plain three-term step: packed arithmetic
                                 const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
-                                const float2 p1 = make_float2(stg1[ml * KT + q], stg1[(ml + 1) * KT + q]);
-                                float2 p2 = make_float2(stg2[ml * KT + q], stg2[(ml + 1) * KT + q]);
+                                const float2 p1 = reinterpret_cast<const float2 *>(stg1)[(ml >> 1) * KT + q];
+                                float2 p2 = reinterpret_cast<const float2 *>(stg2)[(ml >> 1) * KT + q];
                                 unsigned ea = 0, eb = 0;  // extended range: exponents of P_{l-1} at m, m+1
                                 if (EXT) {
                                     ea = ebits(stge1[ml], q);
@@ -790,10 +793,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                         --eb;
                                     }
                                 }
-                                if (wrows) {
-                                    rowp[0] = P.x;
-                                    rowp[stride] = P.y;
-                                }
+                                if (wrows) *reinterpret_cast<float2 *>(rowp) = P;
                                 if (EXT && wrows) {
                                     const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
                                     const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
@@ -823,12 +823,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                         } else if (mh == l) {
                                             // the FP64 sectoral seed, rounded once by k_split_sectoral
                                             // into slot l of the P_{l-1} set (EXT: with its exponent)
-                                            Pq = stg1[mlh * KT + q];
+                                            Pq = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
                                             if (EXT) e = ebits(stge1[mlh], q);
                                         } else if (mh == l - 1) {
                                             // P_{l,l-1} = sqrt(2l+1) x P_{l-1,l-1}, rounded once
                                             const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
-                                            const float p1 = stg1[mlh * KT + q];
+                                            const float p1 = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
                                             if (EXT) e = ebits(stge1[mlh], q);
                                             const float tt = fmaf(xh, p1, xl * p1);
                                             Pq = step_once(A_hi, A_lo, 0.f, 0.f, tt, 0.f);
@@ -839,8 +839,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                         } else {  // m <= l - 2: one recurrence step, rounded once
                                             const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
                                             const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
-                                            const float p1 = stg1[mlh * KT + q];
-                                            float p2 = stg2[mlh * KT + q];
+                                            const float p1 = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
+                                            float p2 = stg2[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
                                             if (EXT) {  // exponents of P_{l-1} and P_{l-2}
                                                 e = ebits(stge1[mlh], q);
                                                 const unsigned e2 = ebits(stge2[mlh], q);
@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                                 --e;
                                             }
                                         }
-                                        if (wrows) rowp[h ? stride : 0] = Pq;
+                                        if (wrows) rowp[h] = Pq;
                                         if (EXT && wrows) {
                                             const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
                                             const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
@@ -878,7 +878,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                         }
                         store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
                     }
-                    rowp += 2 * (int64_t)stride;
+                    rowp += 2 * KT;
                 }
             }
             tc05::fence_proxy_async();
@@ -982,7 +982,8 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
     const int64_t i = t * KT + q;
     const SplitPt &pt = c.pts[i];
     const double s = (double)pt.s_hi + (double)pt.s_lo;
-    const size_t set = (size_t)c.stride * c.lrows;
+    const size_t set = (size_t)c.stride * c.lrp;
+    float *rt = c.rows + (size_t)t * KT * c.lrp + 2 * q;  // this point in tile-major, pair-interleaved rows
     double P = (double)P00_SCALED;
     unsigned e = 0;
     for (int l = 1; l < lmax; ++l) {
@@ -1006,7 +1007,7 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
         } else {
             v = (float)P;
         }
-        c.rows[(size_t)k * set + (size_t)l * c.stride + i] = v;
+        rt[(size_t)k * set + (size_t)(l >> 1) * (2 * KT) + (l & 1)] = v;
     }
 }
 
@@ -1312,6 +1313,19 @@ bool tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t d0, ui
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// 3-D tensor [d2][d1][d0] at `base` (pitches p1, p2 bytes), box b0 x b1 x 1
+bool tmap_3d(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t p1,
+             uint64_t p2, uint32_t b0, uint32_t b1) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {d0, d1, d2};
+    const cuuint64_t strides[2] = {p1, p2};
+    const cuuint32_t box[3] = {b0, b1, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, dt, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // autotune cache key: catalog count, sizes and multipoles of a group
 std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
     std::string k = std::to_string(c1 - c0);
@@ -1429,7 +1443,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int b = 0;
         double acc = 0.0;
         for (int c = 0; c < nc; ++c) {
-            const double need = 3.0 * cats[c].stride * cats[c].in.lmax * 4.0;
+            const double need = 3.0 * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * 4.0;
             bool shared = false;  // pieces of one catalog share f: never in one level launch
             for (int q = b; q < c; ++q) shared |= (cats[q].in.f_acc == cats[c].in.f_acc);
             if (c > b && (acc + need > row_budget || shared)) {
@@ -1463,7 +1477,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             off_pts[c - c0] = ws_bytes;
             ws_bytes += al256((size_t)cats[c].stride * sizeof(SplitPt));
             off_rows[c - c0] = ws_bytes;
-            ws_bytes += al256((size_t)3 * cats[c].stride * cats[c].in.lmax * sizeof(float));
+            ws_bytes += al256((size_t)3 * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * sizeof(float));
             off_exp[c - c0] = ws_bytes;
             if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
         }
@@ -1506,16 +1520,18 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         };
         std::vector<size_t> o_kz(gn), o_nl(gn), o_tm(gn);
         for (int c = c0; c < c1; ++c) {
-            // TMA descriptors: the three Legendre row sets ([lmax][stride] FP32, 32 x 32 boxes)
+            // TMA descriptors: the three Legendre row sets (tile-major, m pairs interleaved:
+            // [tile][lrp / 2][64] FP32, 64 x 16 x 1 boxes = 32 m x 32 points, 4 KB contiguous)
             // and, extended range, the three exponent sets ([tile][epitch] words, 128 x 1 boxes)
             CatPlan &P = cats[c];
             CUtensorMap tm[6];
             memset(tm, 0, sizeof(tm));
             char *rows = ws + off_rows[c - c0];
-            const size_t set_bytes = (size_t)P.stride * P.in.lmax * sizeof(float);
+            const uint64_t lrp = (uint64_t)((P.in.lmax + 1) & ~1);
+            const size_t set_bytes = (size_t)P.stride * lrp * sizeof(float);
             for (int k = 0; k < 3; ++k)
-                if (!tmap_2d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, (uint64_t)P.stride,
-                             (uint64_t)P.in.lmax, (uint64_t)P.stride * sizeof(float), 32, 32)) {
+                if (!tmap_3d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, 2 * KT, lrp / 2,
+                             (uint64_t)P.ntiles, 2 * KT * sizeof(float), lrp * KT * sizeof(float), 2 * KT, 16)) {
                     set_error("cuTensorMapEncodeTiled failed for the Legendre rows");
                     return CATANA_ERR_CUDA;
                 }
@@ -1572,6 +1588,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.n = P.in.n;
             sc.stride = (int)P.stride;
             sc.lrows = P.in.lmax;
+            sc.lrp = (P.in.lmax + 1) & ~1;
             sc.kzw = P.in.nmax;
             sc.epitch = (P.in.lmax + 1) & ~1;
             sc.rexp = ext ? reinterpret_cast<unsigned long long *>(ws + off_exp[c - c0]) : nullptr;
