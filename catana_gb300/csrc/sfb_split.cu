@@ -88,20 +88,25 @@ constexpr uint64_t WAIT_NS = 1000000000ull;  // drains of in-flight copies and M
 constexpr uint32_t SM_J = 8192;          // J hi or J lo: 4 k-groups x 2 atoms
 constexpr uint32_t SM_Y = 16384;         // Y hi or Y lo: 4 k-groups x 4 atoms (256 columns)
 constexpr uint32_t SM_BUF = 2 * SM_J + 2 * SM_Y;
-constexpr uint32_t OFF_ST = 2 * SM_BUF;                // staged Legendre rows, two stages
+constexpr uint32_t OFF_ST = 2 * SM_BUF;                // staged tiles: NST stages (2 or 3)
 constexpr uint32_t SM_STROW = MBLK * KT * 4;           // one row set (MBLK m x 32 points) = 16 KB
 constexpr uint32_t SM_STPTS = KT * 48;                 // the tile's 32 SplitPt records
 constexpr uint32_t SM_STEXP = 2 * MBLK * 8;            // row exponent words of P_{l-1}, P_{l-2} (extended range)
-constexpr uint32_t SM_STAGE = 2 * SM_STROW + SM_STPTS + SM_STEXP;  // P_{l-1}, P_{l-2}, the points, exponents
-constexpr uint32_t OFF_TAB = OFF_ST + 2 * SM_STAGE;
-constexpr uint32_t SM_TAB = NINT_MAX * 32;
-constexpr uint32_t OFF_KZ = OFF_TAB + SM_TAB;          // per n pair: (kz_hi, kz_lo) x 2, then J scales
-constexpr uint32_t OFF_JS = OFF_KZ + NHALF * 8;         // J scale 2^s_ln per n
-constexpr uint32_t OFF_INV = OFF_JS + NHALF * 4;        // readout 2^-s_ln 2^-12 per n
-constexpr uint32_t OFF_COEF = OFF_INV + NHALF * 4;      // recurrence coefficients, m pairs
-constexpr uint32_t OFF_JT = OFF_COEF + MBLK * 16;       // per operand warp: Taylor coefficients of its 8 J rows
-constexpr uint32_t SMEM_BYTES = OFF_JT + (NTHR / 32) * 32 * 4 + 1024;  // + alignment slack
-static_assert(SMEM_BYTES <= 232448, "k_split_l shared memory");
+// one stage: P_{l-1}, P_{l-2}, the points (and, extended range, the exponent words)
+__host__ __device__ constexpr uint32_t sm_stage(bool ext) { return 2 * SM_STROW + SM_STPTS + (ext ? SM_STEXP : 0u); }
+// after the stages: per n pair (kz_hi, kz_lo) x 2; J scale 2^s_ln per n; readout 2^-s_ln 2^-12 per
+// n; recurrence coefficients of the m pairs; per operand warp the Taylor coefficients of its 8 J
+// rows; last, the j_l table of the launch (its interval count sets the dynamic size)
+__host__ __device__ constexpr uint32_t off_kz(bool ext, int nst) { return OFF_ST + (uint32_t)nst * sm_stage(ext); }
+__host__ __device__ constexpr uint32_t off_js(bool ext, int nst) { return off_kz(ext, nst) + NHALF * 8; }
+__host__ __device__ constexpr uint32_t off_inv(bool ext, int nst) { return off_js(ext, nst) + NHALF * 4; }
+__host__ __device__ constexpr uint32_t off_coef(bool ext, int nst) { return off_inv(ext, nst) + NHALF * 4; }
+__host__ __device__ constexpr uint32_t off_jt(bool ext, int nst) { return off_coef(ext, nst) + MBLK * 16; }
+__host__ __device__ constexpr uint32_t off_tab(bool ext, int nst) { return off_jt(ext, nst) + (NTHR / 32) * 32 * 4; }
+// dynamic shared memory of a launch (+ 1024 B of alignment slack)
+constexpr uint32_t smem_bytes(bool ext, int nst, int nint) { return off_tab(ext, nst) + (uint32_t)nint * 32 + 1024; }
+constexpr uint32_t SMEM_LIMIT = 232448 - 1024;  // per block, leaving room for the static part
+static_assert(smem_bytes(true, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
 // J of a tile comes from a cubic Taylor expansion about its record-16 radius when
 // k_max max|r - r_c| <= JT_TAU: the omitted terms are below JT_TAU^4 / 24 ~ 7e-9 of j_l's
 // envelope (the interpolant's derivatives are bounded by it)
@@ -282,15 +287,16 @@ __device__ __forceinline__ float2 step_once2(float2 ah, float2 al, float2 bh, fl
     return __fadd2_rn(s, __fadd2_rn(se, __fadd2_rn(p_lo, __ffma2_rn(al, tt, neg2(q_lo)))));
 }
 
-template <bool EXT, bool FULLJ>
+template <bool EXT, bool FULLJ, int NST>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
+    constexpr uint32_t STG = sm_stage(EXT);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ uint64_t mbar[2];  // MMA completion per operand buffer
-    __shared__ uint64_t sbar[2];  // TMA completion per stage
+    __shared__ uint64_t sbar[NST];  // TMA completion per stage
     __shared__ uint32_t tmem_base_sh;
     __shared__ uint64_t fbar[2];   // operands of buffer b written (NTHR arrivals)
-    __shared__ uint64_t gfree[2];  // stage s read by every operand thread (NTHR arrivals)
+    __shared__ uint64_t gfree[NST];  // stage s read by every operand thread (NTHR arrivals)
     __shared__ int abort_sh;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -308,11 +314,11 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     while ((int)half_cols < ncols_pad) half_cols <<= 1;
     const uint32_t tcols = 2 * half_cols;  // D_tile at column 0, D_acc at column half_cols
 
-    float4 *s_tab = reinterpret_cast<float4 *>(sm + OFF_TAB);
-    float4 *s_kzp = reinterpret_cast<float4 *>(sm + OFF_KZ);  // n pair j: (hi n, hi n+1, lo n, lo n+1)
-    float *s_js = reinterpret_cast<float *>(sm + OFF_JS);
-    float *s_inv = reinterpret_cast<float *>(sm + OFF_INV);
-    float4 *s_coef = reinterpret_cast<float4 *>(sm + OFF_COEF);  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
+    float4 *s_tab = reinterpret_cast<float4 *>(sm + off_tab(EXT, NST));
+    float4 *s_kzp = reinterpret_cast<float4 *>(sm + off_kz(EXT, NST));  // n pair j: (hi n, hi n+1, lo n, lo n+1)
+    float *s_js = reinterpret_cast<float *>(sm + off_js(EXT, NST));
+    float *s_inv = reinterpret_cast<float *>(sm + off_inv(EXT, NST));
+    float4 *s_coef = reinterpret_cast<float4 *>(sm + off_coef(EXT, NST));  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     const float kmax_j = nmax > 0 ? kz_row[nmax - 1].x : 0.f;  // largest k_ln / H of this half (k grows with n)
     for (int t = tid; t < 2 * a.nint; t += NTOT) s_tab[t] = a.tab[t];
@@ -335,12 +341,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     if (tid == 0) {
         tc05::mbar_init(&mbar[0], 1);
         tc05::mbar_init(&mbar[1], 1);
-        tc05::mbar_init(&sbar[0], 1);
-        tc05::mbar_init(&sbar[1], 1);
+        for (int k = 0; k < NST; ++k) tc05::mbar_init(&sbar[k], 1);
         tc05::mbar_init(&fbar[0], NTHR);
         tc05::mbar_init(&fbar[1], NTHR);
-        tc05::mbar_init(&gfree[0], NTHR);
-        tc05::mbar_init(&gfree[1], NTHR);
+        for (int k = 0; k < NST; ++k) tc05::mbar_init(&gfree[k], NTHR);
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -382,7 +386,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     float *__restrict__ partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
-    uint32_t sfill0 = 0, sfill1 = 0, swait0 = 0, swait1 = 0;  // stage loads issued / waited
+    int64_t iss = 0, wtd = 0;  // stage loads issued / waited (tiles of the item, counted from t0)
     bool acc_fresh = true;   // next fold overwrites D_acc
     bool first_flush = true; // partial rows not yet written by this CTA
     int folds = 0;
@@ -398,7 +402,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         return true;
     };
 
-    // stage tile t into stage t&1, all by one thread, completing on sbar[t&1]: the point
+    // stage tile t0 + j into stage j % NST, all by one thread, completing on sbar[j % NST]: the point
     // records (one bulk copy), the rows P_{l-1}(m) and P_{l-2}(m) of this block's m in
     // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
     // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
@@ -417,12 +421,13 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             tc05::tmap_acquire(tm_e2);
         }
     }
-    auto prefetch_rows = [&](int64_t t) {
+    auto prefetch = [&](int64_t j) {
+        const int64_t t = t0 + j;
         if (t >= t1) return;
-        const int sidx = (int)(t & 1);
-        if (sidx) ++sfill1; else ++sfill0;
+        iss = j + 1;
         if (tid != 0) return;
-        uint8_t *stg = sm + OFF_ST + (uint32_t)sidx * SM_STAGE;
+        const int sidx = (int)(j % NST);
+        uint8_t *stg = sm + OFF_ST + (uint32_t)sidx * STG;
         tc05::fence_proxy_async();  // earlier generic reads of this stage before the async writes
         tc05::mbar_arrive_expect_tx(&sbar[sidx], stage_bytes);
         tc05::bulk_g2s(stg + 2 * SM_STROW, cat.pts + t * KT, SM_STPTS, &sbar[sidx]);
@@ -435,10 +440,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
         }
     };
-    auto wait_stage = [&](int sidx, uint64_t limit) -> bool {
-        uint32_t &sw = sidx ? swait1 : swait0;
-        if (!tc05::mbar_wait(&sbar[sidx], sw & 1u, limit)) return false;
-        ++sw;
+    // the load of tile t0 + j is the (j / NST)-th completion of its stage's barrier
+    auto wait_stage = [&](int64_t j, uint64_t limit) -> bool {
+        if (!tc05::mbar_wait(&sbar[j % NST], (uint32_t)((j / NST) & 1), limit)) return false;
+        wtd = j + 1;
         return true;
     };
 
@@ -511,39 +516,38 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // thread (it may be refilled).  Every wait is bounded; a failed one raises abort_sh.
     volatile int *abort_v = &abort_sh;
     if (warp < NTHR / 32) {
-        uint32_t gw0 = 0, gw1 = 0;  // gfree phases waited (thread 0)
-        prefetch_rows(t0);
+        for (int64_t jp = 0; jp + 1 < NST; ++jp) prefetch(jp);  // NST - 1 tiles ahead
         for (int64_t t = t0; t < t1; ++t) {
+            const int64_t j = t - t0;
             if (*abort_v) {
                 ok = false;
                 break;
             }
-            const int b = (int)((t - t0) & 1);
+            const int b = (int)(j & 1);
             bool okp = true;
-            if (tid == 0 && t > t0 && t + 1 < t1) {  // stage (t+1)&1 last held tile t-1
-                uint32_t &gw = ((t + 1) & 1) ? gw1 : gw0;
-                okp = tc05::mbar_wait(&gfree[(t + 1) & 1], gw & 1, a.wait_ns);
-                ++gw;
+            if (tid == 0 && j >= 1 && t + NST - 1 < t1) {  // stage (j-1) % NST last held tile j-1
+                okp = tc05::mbar_wait(&gfree[(j - 1) % NST], (uint32_t)(((j - 1) / NST) & 1), a.wait_ns);
             }
             if (!okp) {
                 *abort_v = 1;
                 ok = false;
                 break;
             }
-            prefetch_rows(t + 1);
-            if (!(wait_buf(b, a.wait_ns) && wait_stage((int)(t & 1), a.wait_ns))) {
+            prefetch(j + NST - 1);
+            if (!(wait_buf(b, a.wait_ns) && wait_stage(j, a.wait_ns))) {
                 *abort_v = 1;
                 ok = false;
                 break;
             }
+            const int sidx = (int)(j % NST);
             uint8_t *bufp = sm + b * SM_BUF;
             uint8_t *jhi = bufp, *jlo = bufp + SM_J, *yhi = bufp + 2 * SM_J, *ylo = bufp + 2 * SM_J + SM_Y;
-            const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE);
+            const float *stg1 = reinterpret_cast<const float *>(sm + OFF_ST + (uint32_t)sidx * STG);
             const float *stg2 = stg1 + MBLK * KT;
             const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
-                sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE + 2 * SM_STROW + SM_STPTS);
+                sm + OFF_ST + (uint32_t)sidx * STG + 2 * SM_STROW + SM_STPTS);
             const unsigned long long *stge2 = stge1 + MBLK;
-            const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+            const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                     2 * SM_STROW + q * 48);
             const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
             // ---- J tile: n = 8 g .. 8 g + 7 ----
@@ -552,13 +556,13 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const float2 w2 = make_float2(pt.w, pt.w);
                 const int n0 = 8 * g;
                 float2 v[4];
-                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // the same for every thread of the CTA
                     // J(n, q) = w_q sum_j c'_j dr_q^j about the tile's record-16 radius r_c:
                     // c'_j = 2^s_n k_n^j p^(j)(u0_n) / j!, p the interval polynomial, u0_n the
                     // offset of z_n = k_n r_c in its interval (float-float product)
-                    float *cs = reinterpret_cast<float *>(sm + OFF_JT) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, NST)) + 32 * g;
                     __syncwarp();
                     if (lane < 8) {
                         const int n = n0 + lane;
@@ -645,10 +649,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(pt.w, pt.w);
-                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)(t & 1) * SM_STAGE +
+                const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
-                    float *cs = reinterpret_cast<float *>(sm + OFF_JT) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, NST)) + 32 * g;
                     __syncwarp();
                     if (lane < 2 * (jp1 - jp0)) {  // rows past the count have k = 0, J scale 0: zero coefficients
                         const int n = 2 * jp0 + lane;
@@ -882,14 +886,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 }
             }
             tc05::fence_proxy_async();
-            ws_arrive(&gfree[t & 1]);
+            ws_arrive(&gfree[sidx]);
             if (!(a.stall && t == t0)) ws_arrive(&fbar[b]);  // the test hook withholds the first hand-off
             if (b) ++uses1; else ++uses0;
         }
         // stage loads still in flight (a loop that stopped early) land before the CTA exits
-        while (swait0 < sfill0 && wait_stage(0, WAIT_NS)) {
-        }
-        while (swait1 < sfill1 && wait_stage(1, WAIT_NS)) {
+        while (wtd < iss && wait_stage(wtd, WAIT_NS)) {
         }
     } else {
         uint32_t fw0 = 0, fw1 = 0;  // fbar phases waited
@@ -1363,14 +1365,11 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     // the test hook (catana_gpu_test_split_stall) arms one run
     const uint64_t stall_ns = g_split_stall_ns.exchange(0);
     if (!ctx->attr_split) {
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES));
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES));
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES));
-        CG_CUDA_TRY(cudaFuncSetAttribute(k_split_l<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES));
+        void (*const kerns[])(SplitArgs) = {k_split_l<false, true, 2>, k_split_l<false, false, 2>,
+                                            k_split_l<false, true, 3>, k_split_l<false, false, 3>,
+                                            k_split_l<true, true, 2>,  k_split_l<true, false, 2>};
+        for (auto kf : kerns)
+            CG_CUDA_TRY(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
         ctx->attr_split = true;
     }
     // ---- extents: max r and max |w| per catalog (one synchronisation) ----
@@ -1460,11 +1459,16 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int lmax_g = 0;
         for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
+        // three stages (tiles staged two ahead) where shared memory allows: plain rows and a
+        // table of at most ~750 intervals; otherwise two
+        const int nst = (!ext && smem_bytes(false, 3, nint) <= SMEM_LIMIT) ? 3 : 2;
+        const uint32_t smem = smem_bytes(ext, nst, nint);
         // kernel per level: extended-range rows above lmax 256; the full-J layout when every
         // item of the level has 128 radial orders in its half
         auto kern_for = [&](bool full) {
-            return ext ? (full ? k_split_l<true, true> : k_split_l<true, false>)
-                       : (full ? k_split_l<false, true> : k_split_l<false, false>);
+            if (ext) return full ? k_split_l<true, true, 2> : k_split_l<true, false, 2>;
+            if (nst == 3) return full ? k_split_l<false, true, 3> : k_split_l<false, false, 3>;
+            return full ? k_split_l<false, true, 2> : k_split_l<false, false, 2>;
         };
         // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
@@ -1715,7 +1719,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         auto level_args = [&](const Sched &S, int l) {
             SplitArgs a;
             a.l = l;
-            a.nint = nint_tab;
+            a.nint = nint;  // intervals this run reaches (the cached table may hold more; its row stride is nint_tab)
             a.items = reinterpret_cast<const SplitItem *>(pd + o_items) + S.item0[l];
             a.cats = reinterpret_cast<const SplitCat *>(pd + o_cats);
             a.coef = coef_d + (size_t)l * (l + 1) / 2;
@@ -1754,7 +1758,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                             if (l >= lmax_g) continue;
                             const int ni = S.item0[l + 1] - S.item0[l];
                             if (ni == 0) continue;
-                            kern_for(S.fullj[l] != 0)<<<ni, NTOT, SMEM_BYTES, st>>>(level_args(S, l));
+                            kern_for(S.fullj[l] != 0)<<<ni, NTOT, smem, st>>>(level_args(S, l));
                             count_launch();
                         }
                         CG_CUDA_TRY(cudaGetLastError());
@@ -1799,7 +1803,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const int nr = S.red0[l + 1] - S.red0[l];
                 if (ni == 0) continue;
                 if (profile) prof_begin(ls_st);
-                kern_for(S.fullj[l] != 0)<<<ni, NTOT, SMEM_BYTES, ls_st>>>(level_args(S, l));
+                kern_for(S.fullj[l] != 0)<<<ni, NTOT, smem, ls_st>>>(level_args(S, l));
                 if (profile) prof_end(ls_st, S.flops[l]);
                 dim3 rg(ceil_div((int64_t)(l + 1) * S.maxn[l], 128), nr);
                 k_split_reduce<<<rg, 128, 0, ls_st>>>(partial, l + 1,
