@@ -593,6 +593,9 @@ def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
     # modes above the 1e-6 bar, by number: how small their C_ln is against the median
     # C of their l (a chi-square draw far below the median inflates the relative error)
     ratio = (c_p / np.median(c_p, axis=1, keepdims=True))[over]
+    ls_over = np.nonzero(over)[0]
+    worst = np.argsort(rel, axis=None)[::-1][:8]
+    med_l = np.median(c_p, axis=1)
     return {
         "sample_points": a.points, "lmax": L, "nmax": M,
         "reference": "FP64 plain GPU path, j_l from piecewise FP64 polynomials (CATANA_JL_POLY), same catalog",
@@ -602,6 +605,12 @@ def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
         "c_ln_modes": int(rel.size), "c_ln_modes_above_1e-6": int(over.sum()),
         "c_ln_above_1e-6_c_over_median_c_l_max": float(ratio.max()) if ratio.size else None,
         "c_ln_above_1e-6_c_over_median_c_l_median": float(np.median(ratio)) if ratio.size else None,
+        "c_ln_above_1e-6_l_min_median_max": ([int(ls_over.min()), float(np.median(ls_over)), int(ls_over.max())]
+                                             if ls_over.size else None),
+        "c_ln_worst_modes": [{"l": int(i // M), "n": int(i % M), "rel_err": float(rel.flat[i]),
+                              "c_over_median_c_l": float(c_p.flat[i] / med_l[i // M]),
+                              "abs_err_over_median_c_l": float(abs(c_s.flat[i] - c_p.flat[i]) / med_l[i // M])}
+                             for i in worst],
         "c_ln_abs_err_over_max_c_or_median_c_l_max": float(typ.max()),
         "f_lmn_max_abs_err_over_max_f": float(np.max(np.abs(fs - fp)) / np.max(np.abs(fp))),
         "f_lmn_rms_err_over_rms_f_by_l": {"l=0": float(rms_l[0]), "l=%d" % (L // 2): float(rms_l[L // 2]),

@@ -132,8 +132,8 @@ static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 // One catalog (or catalog chunk) of a split-form plan.
 struct SplitCat {
     const SplitPt *pts;     // radius-sorted point records, padded to whole tiles
-    float *rows;            // three Legendre row sets, tile-major with m pairs interleaved: value (m, point
-                            // 32 t + q) of set k at rows + k * stride * lrp + t * 32 lrp + 64 (m / 2) + 2 q + m % 2
+    float *rows;            // three Legendre row sets with m pairs interleaved per point: value (m, i) of
+                            // set k at rows + k * stride * lrp + 2 stride (m / 2) + 2 i + m % 2
     int64_t n;              // points
     int stride;             // row stride (multiple of 32, >= n)
     int lrows;              // rows per set (the catalog's lmax)
@@ -431,10 +431,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         tc05::fence_proxy_async();  // earlier generic reads of this stage before the async writes
         tc05::mbar_arrive_expect_tx(&sbar[sidx], stage_bytes);
         tc05::bulk_g2s(stg + 2 * SM_STROW, cat.pts + t * KT, SM_STPTS, &sbar[sidx]);
-        // 32 m (16 interleaved pairs) x 32 points per box: 4 KB contiguous in the tile-major rows
-        for (int k = 0; k < nb1; ++k) tc05::tma_load_3d(stg + k * 4096, tm_r1, 0, (mb0 >> 1) + 16 * k, (int)t, &sbar[sidx]);
+        // 32 m (16 interleaved pairs) x 32 points per box: 16 row segments of 256 B
+        for (int k = 0; k < nb1; ++k) tc05::tma_load_2d(stg + k * 4096, tm_r1, (int)(2 * KT * t), (mb0 >> 1) + 16 * k, &sbar[sidx]);
         for (int k = 0; k < nb2; ++k)
-            tc05::tma_load_3d(stg + SM_STROW + k * 4096, tm_r2, 0, (mb0 >> 1) + 16 * k, (int)t, &sbar[sidx]);
+            tc05::tma_load_2d(stg + SM_STROW + k * 4096, tm_r2, (int)(2 * KT * t), (mb0 >> 1) + 16 * k, &sbar[sidx]);
         if (EXT && l > 0) {
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 float2 cm = make_float2(cma, fmaf(cma, c1, -sma * s1));
                 float2 nsm = make_float2(-sma, -fmaf(sma, c1, cma * s1));
                 // P_l of the pair (m, m + 1) at this point (m even: the pair is one float2)
-                float *rowp = st0 + (size_t)t * KT * cat.lrp + (size_t)(mb0 + mlo) * KT + 2 * q;
+                float *rowp = st0 + (size_t)((mb0 + mlo) >> 1) * 2 * stride + 2 * i;
                 const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
                 const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
                 const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
@@ -882,7 +882,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                         }
                         store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
                     }
-                    rowp += 2 * KT;
+                    rowp += 2 * (size_t)stride;
                 }
             }
             tc05::fence_proxy_async();
@@ -985,7 +985,7 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
     const SplitPt &pt = c.pts[i];
     const double s = (double)pt.s_hi + (double)pt.s_lo;
     const size_t set = (size_t)c.stride * c.lrp;
-    float *rt = c.rows + (size_t)t * KT * c.lrp + 2 * q;  // this point in tile-major, pair-interleaved rows
+    float *rt = c.rows + 2 * i;  // this point in the pair-interleaved rows
     double P = (double)P00_SCALED;
     unsigned e = 0;
     for (int l = 1; l < lmax; ++l) {
@@ -1009,7 +1009,7 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
         } else {
             v = (float)P;
         }
-        rt[(size_t)k * set + (size_t)(l >> 1) * (2 * KT) + (l & 1)] = v;
+        rt[(size_t)k * set + (size_t)(l >> 1) * 2 * c.stride + (l & 1)] = v;
     }
 }
 
@@ -1315,19 +1315,6 @@ bool tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t d0, ui
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// 3-D tensor [d2][d1][d0] at `base` (pitches p1, p2 bytes), box b0 x b1 x 1
-bool tmap_3d(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t p1,
-             uint64_t p2, uint32_t b0, uint32_t b1) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
-    if (!enc) return false;
-    const cuuint64_t dims[3] = {d0, d1, d2};
-    const cuuint64_t strides[2] = {p1, p2};
-    const cuuint32_t box[3] = {b0, b1, 1};
-    const cuuint32_t es[3] = {1, 1, 1};
-    return enc(m, dt, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 // autotune cache key: catalog count, sizes and multipoles of a group
 std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
     std::string k = std::to_string(c1 - c0);
@@ -1524,8 +1511,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         };
         std::vector<size_t> o_kz(gn), o_nl(gn), o_tm(gn);
         for (int c = c0; c < c1; ++c) {
-            // TMA descriptors: the three Legendre row sets (tile-major, m pairs interleaved:
-            // [tile][lrp / 2][64] FP32, 64 x 16 x 1 boxes = 32 m x 32 points, 4 KB contiguous)
+            // TMA descriptors: the three Legendre row sets (m pairs interleaved per point:
+            // [lrp / 2][2 stride] FP32, 64 x 16 boxes = 32 m x 32 points)
             // and, extended range, the three exponent sets ([tile][epitch] words, 128 x 1 boxes)
             CatPlan &P = cats[c];
             CUtensorMap tm[6];
@@ -1534,8 +1521,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             const uint64_t lrp = (uint64_t)((P.in.lmax + 1) & ~1);
             const size_t set_bytes = (size_t)P.stride * lrp * sizeof(float);
             for (int k = 0; k < 3; ++k)
-                if (!tmap_3d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, 2 * KT, lrp / 2,
-                             (uint64_t)P.ntiles, 2 * KT * sizeof(float), lrp * KT * sizeof(float), 2 * KT, 16)) {
+                if (!tmap_2d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, 2 * (uint64_t)P.stride,
+                             lrp / 2, 2 * (uint64_t)P.stride * sizeof(float), 2 * KT, 16)) {
                     set_error("cuTensorMapEncodeTiled failed for the Legendre rows");
                     return CATANA_ERR_CUDA;
                 }

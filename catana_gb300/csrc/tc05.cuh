@@ -139,15 +139,6 @@ __device__ __forceinline__ void tma_load_2d(void *dst_smem, const void *tmap, in
         : "memory");
 }
 
-// 3-D tiled TMA load of one box at element coordinates (x, y, z).
-__device__ __forceinline__ void tma_load_3d(void *dst_smem, const void *tmap, int x, int y, int z, uint64_t *mbar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst_smem)),
-        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(mbar))
-        : "memory");
-}
-
 // 32 lanes x 16 consecutive 32-bit columns from TMEM (this warp's lane quadrant).
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
