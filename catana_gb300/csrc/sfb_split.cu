@@ -82,6 +82,7 @@ constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 
 constexpr int SPLIT_LMAX_EXT = 512; // with the 2-bit row exponents (extended range)
 constexpr int SPLIT_NMAX = 256;     // two 128-lane halves (separate work items)
 constexpr int NHALF = 128;          // radial orders per work item (accumulator lanes)
+constexpr int MR_STD = 128;         // plain form: columns m >= MR_STD keep the three-term step
 constexpr uint64_t WAIT_NS = 1000000000ull;  // drains of in-flight copies and MMAs before exit (1 s)
 
 // shared-memory map (bytes, from a 1024-aligned base)
@@ -101,7 +102,8 @@ __host__ __device__ constexpr uint32_t off_kz(bool ext, int nst) { return OFF_ST
 __host__ __device__ constexpr uint32_t off_js(bool ext, int nst) { return off_kz(ext, nst) + NHALF * 8; }
 __host__ __device__ constexpr uint32_t off_inv(bool ext, int nst) { return off_js(ext, nst) + NHALF * 4; }
 __host__ __device__ constexpr uint32_t off_coef(bool ext, int nst) { return off_inv(ext, nst) + NHALF * 4; }
-__host__ __device__ constexpr uint32_t off_jt(bool ext, int nst) { return off_coef(ext, nst) + MBLK * 16; }
+__host__ __device__ constexpr uint32_t off_rcoef(bool ext, int nst) { return off_coef(ext, nst) + MBLK * 16; }
+__host__ __device__ constexpr uint32_t off_jt(bool ext, int nst) { return off_rcoef(ext, nst) + (ext ? 0u : MBLK * 16); }
 __host__ __device__ constexpr uint32_t off_tab(bool ext, int nst) { return off_jt(ext, nst) + (NTHR / 32) * 32 * 4; }
 // dynamic shared memory of a launch (+ 1024 B of alignment slack)
 constexpr uint32_t smem_bytes(bool ext, int nst, int nint) { return off_tab(ext, nst) + (uint32_t)nint * 32 + 1024; }
@@ -121,8 +123,8 @@ constexpr float Y_SCALE = 4096.0f;                    // 2^12
 // Per-point operand inputs of the split form (48 bytes, radius-sorted order).
 struct SplitPt {
     float r_hi, r_lo, w;        // radius (float-float), weight
-    float x_hi, x_lo;           // cos(theta) (float-float)
-    float s_hi, s_lo;           // sin(theta) (float-float)
+    float x_hi, x_lo;           // cos(theta), plain form |cos(theta)| (float-float)
+    float s_hi, s_lo;           // sin(theta), plain form 1 - |cos(theta)| (float-float)
     float cphi, sphi;           // e^{i phi}
     float dr;                   // r - r of the tile's record 16; record 16 itself: max |dr| of the tile
     unsigned long long u;       // phi / 2pi as a 64-bit fraction of a turn
@@ -132,8 +134,10 @@ static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 // One catalog (or catalog chunk) of a split-form plan.
 struct SplitCat {
     const SplitPt *pts;     // radius-sorted point records, padded to whole tiles
-    float *rows;            // three Legendre row sets with m pairs interleaved per point: value (m, i) of
-                            // set k at rows + k * stride * lrp + 2 stride (m / 2) + 2 i + m % 2
+    float *rows;            // Legendre row sets with m pairs interleaved per point: value (m, i) of set k
+                            // at rows + k * stride * lrp + 2 stride (m / 2) + 2 i + m % 2.  Plain form:
+                            // sets 0, 1 = P_l by the parity of l, sets 2, 3 = X_l likewise; extended
+                            // range: sets l % 3 = P_l
     int64_t n;              // points
     int stride;             // row stride (multiple of 32, >= n)
     int lrows;              // rows per set (the catalog's lmax)
@@ -157,7 +161,8 @@ struct SplitArgs {
     int l, nint;
     const SplitItem *items;  // this level's items (one per CTA)
     const SplitCat *cats;
-    const float4 *coef;      // recurrence coefficients, row l
+    const float4 *coef;      // recurrence coefficients (A, B as float-float), row l
+    const float4 *rcoef;     // Reinsch-modified step (c1, rho as float-float), row l
     const float4 *tab;       // j_l table, row l: nint intervals x 2 float4
     float *partial;          // [item][256][128]
     int *err;
@@ -287,6 +292,28 @@ __device__ __forceinline__ float2 step_once2(float2 ah, float2 al, float2 bh, fl
     return __fadd2_rn(s, __fadd2_rn(se, __fadd2_rn(p_lo, __ffma2_rn(al, tt, neg2(q_lo)))));
 }
 
+// rho p + d rounded once (rho = rh + rl as float-float): TwoProduct of rh p and TwoSum with
+// d, plus the remainders.  The column m = 0 of the Reinsch-modified recurrence takes it:
+// the two-fma form rounds rl p + d at the magnitude of d, and near the equator that
+// rounding has a mean over the sphere of ~1e-8 of P_l0 at small l, which a catalog's
+// monopole (a sum growing like N) leaks through into l > 0.
+__device__ __forceinline__ float sum_once(float rh, float rl, float p, float d) {
+    const float ph = __fmul_rn(rh, p);
+    const float pl = fmaf(rh, p, -ph);
+    const float s = __fadd_rn(ph, d);
+    const float v = __fadd_rn(s, -ph);
+    const float se = __fadd_rn(__fadd_rn(ph, -__fadd_rn(s, -v)), __fadd_rn(d, -v));
+    return __fadd_rn(s, __fadd_rn(se, fmaf(rl, p, pl)));
+}
+__device__ __forceinline__ float2 sum_once2(float2 rh, float2 rl, float2 p, float2 d) {
+    const float2 ph = __fmul2_rn(rh, p);
+    const float2 pl = __ffma2_rn(rh, p, neg2(ph));
+    const float2 s = __fadd2_rn(ph, d);
+    const float2 v = __fadd2_rn(s, neg2(ph));
+    const float2 se = __fadd2_rn(__fadd2_rn(ph, neg2(__fadd2_rn(s, neg2(v)))), __fadd2_rn(d, neg2(v)));
+    return __fadd2_rn(s, __fadd2_rn(se, __ffma2_rn(rl, p, pl)));
+}
+
 template <bool EXT, bool FULLJ, int NST>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     constexpr uint32_t STG = sm_stage(EXT);
@@ -319,6 +346,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     float *s_js = reinterpret_cast<float *>(sm + off_js(EXT, NST));
     float *s_inv = reinterpret_cast<float *>(sm + off_inv(EXT, NST));
     float4 *s_coef = reinterpret_cast<float4 *>(sm + off_coef(EXT, NST));  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
+    float4 *s_rcoef = reinterpret_cast<float4 *>(sm + off_rcoef(EXT, NST));  // m pair j: (c1_hi x2, c1_lo x2), (rho_hi x2, rho_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     const float kmax_j = nmax > 0 ? kz_row[nmax - 1].x : 0.f;  // largest k_ln / H of this half (k grows with n)
     for (int t = tid; t < 2 * a.nint; t += NTOT) s_tab[t] = a.tab[t];
@@ -337,6 +365,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         const float4 cb = 2 * t + 1 < mcount ? a.coef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
         s_coef[2 * t] = make_float4(ca.x, cb.x, ca.y, cb.y);
         s_coef[2 * t + 1] = make_float4(ca.z, cb.z, ca.w, cb.w);
+        if (!EXT) {
+            const float4 ra = a.rcoef[mb0 + 2 * t];
+            const float4 rb = 2 * t + 1 < mcount ? a.rcoef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+            s_rcoef[2 * t] = make_float4(ra.x, rb.x, ra.y, rb.y);
+            s_rcoef[2 * t + 1] = make_float4(ra.z, rb.z, ra.w, rb.w);
+        }
     }
     if (tid == 0) {
         tc05::mbar_init(&mbar[0], 1);
@@ -373,9 +407,9 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
     const size_t set = (size_t)stride * cat.lrp;
-    const float *__restrict__ st1 = cat.rows + (size_t)((l + 2) % 3) * set;  // P_{l-1}
-    const float *__restrict__ st2 = cat.rows + (size_t)((l + 1) % 3) * set;  // P_{l-2}
-    float *__restrict__ st0 = cat.rows + (size_t)(l % 3) * set;              // P_l
+    // the rows this level writes: P_l (and, plain form, X_l)
+    float *__restrict__ st0 = cat.rows + (size_t)(EXT ? l % 3 : (l & 1)) * set;
+    float *__restrict__ xt0 = cat.rows + (size_t)(EXT ? 0 : 2 + (l & 1)) * set;
     const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
     unsigned long long *ex0 = nullptr;
     if (EXT) {
@@ -407,10 +441,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
     // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
     // and (extended range) the exponent words of both sets
-    const char *tm_r1 = cat.tmaps + 128 * ((l + 2) % 3), *tm_r2 = cat.tmaps + 128 * ((l + 1) % 3);
+    // staged rows: P_{l-1} and (extended range) P_{l-2} or (plain form) X_{l-1}
+    const char *tm_r1 = cat.tmaps + 128 * (EXT ? (l + 2) % 3 : (l + 1) & 1);
+    const char *tm_r2 = cat.tmaps + 128 * (EXT ? (l + 1) % 3 : 2 + ((l + 1) & 1));
     const char *tm_e1 = cat.tmaps + 128 * (3 + (l + 2) % 3), *tm_e2 = cat.tmaps + 128 * (3 + (l + 1) % 3);
     const int nb1 = l > 0 ? (mcount + 31) >> 5 : 0;
-    const int nb2 = (max(0, min(mcount, l - 1 - mb0)) + 31) >> 5;
+    const int nb2 = (max(0, min(mcount, EXT ? l - 1 - mb0 : l - mb0)) + 31) >> 5;
     const uint32_t stage_bytes =
         SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? 2u * (MBLK * 8) : 0u);
     if (tid == 0) {  // descriptors rewritten by the host between launches: read them afresh
@@ -550,10 +586,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                     2 * SM_STROW + q * 48);
             const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
+            // plain form: rows at |cos(theta)|, the factor (-1)^l of a southern point in its weight
+            const float wq = (!EXT && (l & 1) && (pt.u & 1ull)) ? -pt.w : pt.w;
             // ---- J tile: n = 8 g .. 8 g + 7 ----
             if constexpr (FULLJ) {
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
-                const float2 w2 = make_float2(pt.w, pt.w);
+                const float2 w2 = make_float2(wq, wq);
                 const int n0 = 8 * g;
                 float2 v[4];
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
@@ -648,7 +686,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const int npr = (nmax + 1) >> 1;
                 const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
-                const float2 w2 = make_float2(pt.w, pt.w);
+                const float2 w2 = make_float2(wq, wq);
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
@@ -739,7 +777,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             }
             // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
             if (mlo < mhi) {
-                const float xh = pt.x_hi, xl = pt.x_lo, sh = pt.s_hi, sl = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
+                // x = cos(theta) (plain form: |cos(theta)|) and, plain form, eps = 1 - |cos(theta)|
+                const float xh = pt.x_hi, xl = pt.x_lo, eh = pt.s_hi, el = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
                 // e^{i m phi} for the pair (m, m+1), times the readout factor 2^-88 of the scaled
                 // rows (exact): seed m, one rotation by e^{i phi}; pairs then advance by
                 // e^{2 i phi}.  nsm holds -sin.
@@ -754,6 +793,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const float c2 = fmaf(c1, c1, -s1 * s1), s2 = 2.f * c1 * s1;
                 const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
                 const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
+                const float2 eh2 = make_float2(eh, eh), el2 = make_float2(el, el);
     #pragma unroll
                 for (int pp = 0; pp < 4; ++pp) {
                     const int ml = mlo + 2 * pp;  // even local m
@@ -762,7 +802,86 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                         {
                             const int m = mb0 + ml;
                             float2 P;
-                            if (m + 1 <= l - 2 && ml + 1 < mcount) {
+                            if constexpr (!EXT) {
+                                // plain form: rows P_l and X_l at |cos(theta)|.  Columns m < MR_STD
+                                // take the Reinsch-modified step (X = D_l = P_l - rho_l P_{l-1}):
+                                //   D_l = c1_l D_{l-1} - A_l eps P_{l-1},  P_l = rho_l P_{l-1} + D_l,
+                                // in which near the poles (eps -> 0) D is small and the rounding of
+                                // P_l no longer accumulates through the three-term recurrence's
+                                // cancellation; columns m >= MR_STD (their points lie away from the
+                                // poles) keep the three-term step, X = P_{l-1}
+                                float *xrowp = rowp + (xt0 - st0);
+                                if (m + 1 <= l - 1 && ml + 1 < mcount) {
+                                    const float2 p1 = reinterpret_cast<const float2 *>(stg1)[(ml >> 1) * KT + q];
+                                    const float2 x1 = reinterpret_cast<const float2 *>(stg2)[(ml >> 1) * KT + q];
+                                    const float4 ca = s_coef[ml];
+                                    float2 Xn;
+                                    if (m >= MR_STD) {
+                                        const float4 cb = s_coef[ml + 1];
+                                        const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
+                                        const float2 bb = __ffma2_rn(make_float2(cb.z, cb.w), x1,
+                                                                     __fmul2_rn(make_float2(cb.x, cb.y), x1));
+                                        const float2 vv = __ffma2_rn(make_float2(ca.z, ca.w), tt, neg2(bb));
+                                        P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
+                                        Xn = p1;
+                                    } else {
+                                        const float4 ra = s_rcoef[ml], rb = s_rcoef[ml + 1];
+                                        const float2 u = __ffma2_rn(eh2, p1, __fmul2_rn(el2, p1));
+                                        const float2 corr = __ffma2_rn(make_float2(ra.z, ra.w), x1,
+                                                                       __fmul2_rn(make_float2(-ca.z, -ca.w), u));
+                                        Xn = __ffma2_rn(make_float2(ra.x, ra.y), x1,
+                                                        __ffma2_rn(make_float2(-ca.x, -ca.y), u, corr));
+                                        if (m == 0)
+                                            P = sum_once2(make_float2(rb.x, rb.y), make_float2(rb.z, rb.w), p1, Xn);
+                                        else
+                                            P = __ffma2_rn(make_float2(rb.x, rb.y), p1,
+                                                           __ffma2_rn(make_float2(rb.z, rb.w), p1, Xn));
+                                    }
+                                    if (wrows) {
+                                        *reinterpret_cast<float2 *>(rowp) = P;
+                                        *reinterpret_cast<float2 *>(xrowp) = Xn;
+                                    }
+                                } else {
+                                    // the sectoral m = l (the FP64 seed, X = 0), or the block's last odd m
+                                    const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
+                                    const float4 ra = s_rcoef[ml], rb = s_rcoef[ml + 1];
+                                    float pv[2];
+    #pragma unroll
+                                    for (int h = 0; h < 2; ++h) {
+                                        const int mlh = ml + h, mh = m + h;
+                                        float Pq = 0.f, Xq = 0.f;
+                                        if (mlh < mhi) {  // warp-uniform
+                                            const int si = ((mlh >> 1) * KT + q) * 2 + (mlh & 1);
+                                            if (l == 0) {
+                                                Pq = P00_SCALED;
+                                            } else if (mh == l) {
+                                                Pq = stg1[si];
+                                            } else {
+                                                const float p1 = stg1[si], x1 = stg2[si];
+                                                const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
+                                                if (mh >= MR_STD) {
+                                                    const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
+                                                    Pq = step_once(A_hi, A_lo, B_hi, B_lo, fmaf(xh, p1, xl * p1), x1);
+                                                    Xq = p1;
+                                                } else {
+                                                    const float c_hi = h ? ra.y : ra.x, c_lo = h ? ra.w : ra.z;
+                                                    const float r_hi = h ? rb.y : rb.x, r_lo = h ? rb.w : rb.z;
+                                                    const float u = fmaf(eh, p1, el * p1);
+                                                    Xq = fmaf(c_hi, x1, fmaf(-A_hi, u, fmaf(c_lo, x1, -A_lo * u)));
+                                                    Pq = (mh == 0) ? sum_once(r_hi, r_lo, p1, Xq)
+                                                                   : fmaf(r_hi, p1, fmaf(r_lo, p1, Xq));
+                                                }
+                                            }
+                                            if (wrows) {
+                                                rowp[h] = Pq;
+                                                xrowp[h] = Xq;
+                                            }
+                                        }
+                                        pv[h] = Pq;
+                                    }
+                                    P = make_float2(pv[0], pv[1]);
+                                }
+                            } else if (m + 1 <= l - 2 && ml + 1 < mcount) {
                                 // both m take the plain three-term step: packed arithmetic
                                 const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
                                 const float2 p1 = reinterpret_cast<const float2 *>(stg1)[(ml >> 1) * KT + q];
@@ -983,14 +1102,16 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
     const int q = threadIdx.x & 31;
     const int64_t i = t * KT + q;
     const SplitPt &pt = c.pts[i];
-    const double s = (double)pt.s_hi + (double)pt.s_lo;
+    // sin(theta): stored (extended range), or from eps = 1 - |cos(theta)| as sqrt(eps (2 - eps))
+    const double sv = (double)pt.s_hi + (double)pt.s_lo;
+    const double s = ext ? sv : sqrt(sv * (2.0 - sv));
     const size_t set = (size_t)c.stride * c.lrp;
     float *rt = c.rows + 2 * i;  // this point in the pair-interleaved rows
     double P = (double)P00_SCALED;
     unsigned e = 0;
     for (int l = 1; l < lmax; ++l) {
         P = asect[l] * s * P;
-        const int k = (l + 2) % 3;  // the set of P_{l-1}
+        const int k = ext ? (l + 2) % 3 : (l + 1) & 1;  // the set of P_{l-1}
         float v;
         if (ext) {
             double f = P;
@@ -1050,9 +1171,16 @@ __global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const
 // that record is padding), and record 16 carries the tile's max |dr| instead: the J
 // operand of a tile whose radii lie close together comes from a Taylor expansion
 // about r_c (k_split_l).  One warp per tile (blockDim a multiple of 32).
+// Plain form (rows of the Reinsch-modified recurrence): the rows are evaluated at
+// |cos(theta)|, since P_lm(-x) = (-1)^(l+m) P_lm(x): a point of the southern hemisphere
+// takes phi + pi (the factor (-1)^m of the phase), bit 0 of its phase fraction records
+// the hemisphere and k_split_l applies (-1)^l through its J weight.  The record then
+// carries 1 - |cos(theta)| = 2 sin^2(theta / 2) (north) or 2 cos^2(theta / 2) (south),
+// exact to a relative 1e-16 right up to the poles, in place of sin(theta).
 template <typename T>
 __global__ void k_split_prep(const T *__restrict__ pts, const T *__restrict__ w,
-                             const uint32_t *__restrict__ perm, int64_t n, int64_t npad, SplitPt *out, int *err) {
+                             const uint32_t *__restrict__ perm, int64_t n, int64_t npad, SplitPt *out, int *err,
+                             int plain) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i - (threadIdx.x & 31) >= npad) return;  // whole warps (npad is a multiple of 32)
     const int64_t ic = (i & ~(int64_t)31) + 16;
@@ -1076,17 +1204,27 @@ __global__ void k_split_prep(const T *__restrict__ pts, const T *__restrict__ w,
     sincos(ph, &sp, &cp);
     o.r_hi = (float)r;
     o.r_lo = (float)(r - (double)o.r_hi);
-    o.x_hi = (float)ct;
-    o.x_lo = (float)(ct - (double)o.x_hi);
-    o.s_hi = (float)st;
-    o.s_lo = (float)(st - (double)o.s_hi);
-    o.cphi = (float)cp;
-    o.sphi = (float)sp;
+    const bool south = plain && ct < 0.0;
+    double xv = ct, sv = st;
+    if (plain) {
+        double sh, ch;
+        sincos(0.5 * th, &sh, &ch);
+        xv = fabs(ct);
+        sv = south ? 2.0 * ch * ch : 2.0 * sh * sh;  // 1 - |cos(theta)|
+    }
+    o.x_hi = (float)xv;
+    o.x_lo = (float)(xv - (double)o.x_hi);
+    o.s_hi = (float)sv;
+    o.s_lo = (float)(sv - (double)o.s_hi);
+    o.cphi = (float)(south ? -cp : cp);
+    o.sphi = (float)(south ? -sp : sp);
     o.dr = (threadIdx.x & 31) == 16 ? dmax : (float)dr;
     double f = ph * 0.15915494309189533577;  // phi / 2pi
     f -= floor(f);
     const double scaled = ldexp(f, 64);
-    o.u = scaled >= 18446744073709551615.0 ? 0ull : (unsigned long long)scaled;
+    unsigned long long u = scaled >= 18446744073709551615.0 ? 0ull : (unsigned long long)scaled;
+    if (south) u += 0x8000000000000000ull;  // + half a turn
+    o.u = (u & ~1ull) | (south ? 1ull : 0ull);  // bit 0 (2^-64 of a turn): the hemisphere
     o.w = w ? (float)w[j] : 1.0f;
     out[i] = o;
 }
@@ -1222,7 +1360,8 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
     nint = std::max(nint, C.nint);
     const size_t tab_bytes = (size_t)lmax * nint * 2 * sizeof(float4);
     const size_t coef_bytes = (size_t)lmax * (lmax + 1) / 2 * sizeof(float4);
-    CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + coef_bytes + 1024));
+    // [j_l tables][(A, B) per (l, m)][(c1, rho) per (l, m): the Reinsch-modified step]
+    CG_CUDA_TRY(ctx->split_tab.ensure(tab_bytes + 2 * coef_bytes + 1024));
     constexpr int NC = TDEG + 1;
     const size_t vbytes = (size_t)nint * NC * lmax * sizeof(double);
     DevBuf tmp;
@@ -1238,7 +1377,30 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
     k_split_coefs<<<ceil_div((int64_t)lmax * nint, 128), 128, 0, st>>>(lmax, nint, vals, vinv, tab);
     count_launch();
     CG_CUDA_TRY(cudaGetLastError());
-    std::vector<float4> co((size_t)lmax * (lmax + 1) / 2);
+    std::vector<float4> co((size_t)lmax * (lmax + 1) / 2), ro(co.size(), make_float4(0.f, 0.f, 0.f, 0.f));
+    // Reinsch-modified step of column m: rho_l = Pt_lm(1) / Pt_{l-1,m}(1) (Pt = P / sin^m),
+    // rho_{m+1} = A_{m+1,m}, rho_l = A_l - B_l / rho_{l-1}; c1_l = A_l - rho_l = B_l / rho_{l-1}
+    for (int m = 0; m + 1 < lmax; ++m) {
+        long double rho = 0.0L;
+        for (int l = m + 1; l < lmax; ++l) {
+            const long double dl = l, dl1 = l - 1, mm = (long double)m * m;
+            long double A, B;
+            if (l == m + 1) {
+                A = sqrtl(2.0L * l + 1.0L);
+                B = 0.0L;
+            } else {
+                A = sqrtl((4.0L * dl * dl - 1.0L) / (dl * dl - mm));
+                B = A * sqrtl((dl1 * dl1 - mm) / (4.0L * dl1 * dl1 - 1.0L));
+            }
+            const long double rn = (l == m + 1) ? A : A - B / rho;
+            const long double c1 = (l == m + 1) ? 0.0L : B / rho;
+            float ch, cl, rh, rl;
+            split_ff((double)c1, ch, cl);
+            split_ff((double)rn, rh, rl);
+            ro[(size_t)l * (l + 1) / 2 + m] = make_float4(ch, cl, rh, rl);
+            rho = rn;
+        }
+    }
     for (int l = 0; l < lmax; ++l)
         for (int m = 0; m <= l; ++m) {
             double A = 0.0, B = 0.0;
@@ -1259,6 +1421,8 @@ catana_status_t ensure_split_tables(DeviceContext *ctx, int lmax, int nint, cuda
             co[(size_t)l * (l + 1) / 2 + m] = make_float4(ah, al, bh, bl);
         }
     CG_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(tab) + tab_bytes, co.data(), coef_bytes,
+                                cudaMemcpyHostToDevice, st));
+    CG_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(tab) + tab_bytes + coef_bytes, ro.data(), coef_bytes,
                                 cudaMemcpyHostToDevice, st));
     C.maxj.assign(lmax, 1.0);
     C.zpeak.assign(lmax, 0.0);
@@ -1429,7 +1593,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int b = 0;
         double acc = 0.0;
         for (int c = 0; c < nc; ++c) {
-            const double need = 3.0 * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * 4.0;
+            const double need = 4.0 * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * 4.0;
             bool shared = false;  // pieces of one catalog share f: never in one level launch
             for (int q = b; q < c; ++q) shared |= (cats[q].in.f_acc == cats[c].in.f_acc);
             if (c > b && (acc + need > row_budget || shared)) {
@@ -1446,6 +1610,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int lmax_g = 0;
         for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
+        // row sets: plain form P_l, X_l by the parity of l (X = D or P_{l-1}); extended range
+        // P_l, P_{l-1}, P_{l-2} rotating
+        const int nsets = ext ? 3 : 4;
         // three stages (tiles staged two ahead) where shared memory allows: plain rows and a
         // table of at most ~750 intervals; otherwise two
         const int nst = (!ext && smem_bytes(false, 3, nint) <= SMEM_LIMIT) ? 3 : 2;
@@ -1468,7 +1635,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             off_pts[c - c0] = ws_bytes;
             ws_bytes += al256((size_t)cats[c].stride * sizeof(SplitPt));
             off_rows[c - c0] = ws_bytes;
-            ws_bytes += al256((size_t)3 * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * sizeof(float));
+            ws_bytes += al256((size_t)nsets * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * sizeof(float));
             off_exp[c - c0] = ws_bytes;
             if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
         }
@@ -1494,10 +1661,10 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             const int64_t npad = P.ntiles * KT;
             if (P.in.pts32)
                 k_split_prep<float><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts32, P.in.w32, perm, n, npad, spts,
-                                                                         err_dev);
+                                                                         err_dev, ext ? 0 : 1);
             else
                 k_split_prep<double><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts, P.in.w, perm, n, npad, spts,
-                                                                          err_dev);
+                                                                          err_dev, ext ? 0 : 1);
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
         }
@@ -1520,7 +1687,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             char *rows = ws + off_rows[c - c0];
             const uint64_t lrp = (uint64_t)((P.in.lmax + 1) & ~1);
             const size_t set_bytes = (size_t)P.stride * lrp * sizeof(float);
-            for (int k = 0; k < 3; ++k)
+            for (int k = 0; k < nsets; ++k)
                 if (!tmap_2d(&tm[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rows + k * set_bytes, 2 * (uint64_t)P.stride,
                              lrp / 2, 2 * (uint64_t)P.stride * sizeof(float), 2 * KT, 16)) {
                     set_error("cuTensorMapEncodeTiled failed for the Legendre rows");
@@ -1710,6 +1877,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             a.items = reinterpret_cast<const SplitItem *>(pd + o_items) + S.item0[l];
             a.cats = reinterpret_cast<const SplitCat *>(pd + o_cats);
             a.coef = coef_d + (size_t)l * (l + 1) / 2;
+            a.rcoef = coef_d + (size_t)lmax_tab * (lmax_tab + 1) / 2 + (size_t)l * (l + 1) / 2;
             a.tab = tab + (size_t)l * nint_tab * 2;
             a.partial = ctx->partial.as<float>();
             a.err = err_dev;
