@@ -457,18 +457,28 @@ def streamed_workload(torch, _lib, catana, chunks=2, chunk=8_000_000, L=512, M=2
     tp = time.perf_counter() - t0
     out["plain_fp64_20k_value"] = 20000 * modes(L, M) / tp
     out["split_over_plain"] = out["value"] / out["plain_fp64_20k_value"]
-    # C_l error of the split form against FP64 with exact j_l on 1500 points
-    e = host[0].numpy()[:1500].astype(np.float64)
+    # C_l and f error of the split form against the FP64 plain path (j_l from the FP64
+    # polynomials, as accurate as the exact branch) on the first 100k points of chunk 0
+    ns = 100_000
+    e = host[0].numpy()[:ns].astype(np.float64)
     pe = catana.PointContainer(e)
-    rs = catana.sfb_decomposition(pe, L, M, 1500.0, False, False, precision="split")
-    rp = catana.sfb_decomposition(pe, L, M, 1500.0, False, False, interpolation="off")
+    rs = catana.sfb_decomposition(pe, L, M, 1500.0, True, False, precision="split")
+    rp = catana.sfb_decomposition(pe, L, M, 1500.0, True, False, interpolation="poly")
     rel = np.abs(rs.c_ln - rp.c_ln) / np.abs(rp.c_ln)
     keep = rp.c_ln >= 1e-40 * rp.c_ln.max()  # below: j_l(k r) < ~1e-20 of its envelope at every point
-    out["accuracy_1500pts"] = {"c_ln_rel_err_median": float(np.median(rel)),
-                               "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
-                               "c_ln_rel_err_p99_modes_above_1e-40_cmax": float(np.percentile(rel[keep], 99)),
-                               "modes_below_1e-40_cmax": float(1.0 - keep.mean()),
-                               "reference": "FP64 plain path, exact j_l"}
+    rms_l = [float(np.sqrt(np.mean(np.abs(x - y) ** 2) / np.mean(np.abs(y) ** 2))) for x, y in zip(rs.f_lmn, rp.f_lmn)]
+    out["accuracy_100k_pts"] = {"sample_points": ns,
+                                "c_ln_rel_err_median": float(np.median(rel[keep])),
+                                "c_ln_rel_err_p99": float(np.percentile(rel[keep], 99)),
+                                "c_ln_rel_err_max": float(rel[keep].max()),
+                                "c_ln_modes_above_1e-6": int((rel[keep] > 1e-6).sum()),
+                                "modes_below_1e-40_cmax": float(1.0 - keep.mean()),
+                                "f_lmn_rms_err_over_rms_f_by_l": {"l=0": rms_l[0], "l=%d" % (L // 2): rms_l[L // 2],
+                                                                  "l=%d" % (L - 1): rms_l[-1], "max": max(rms_l)},
+                                "reference": "FP64 plain path, j_l from the FP64 polynomials (CATANA_JL_POLY)",
+                                "note": "C_ln below 1e-40 of the largest C (j_l(k r) < ~1e-20 of its envelope at "
+                                        "every point) leave the FP32 operand range and come out 0; the statistics "
+                                        "cover the modes above"}
     del host
     return out
 
@@ -554,31 +564,8 @@ def torch_device_index():
     return torch.cuda.current_device()
 
 
-def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
-    """The split form's error on the whole catalog: d_f / d_c hold the split result of
-    the last timed step; the same catalog runs once more through the FP64 plain path
-    with j_l from the piecewise FP64 polynomials (CATANA_JL_POLY, pinned to the
-    oracle's exact j_l at 1e-10 of max|f| in tests/test_raw_fp64_gpu.py), and every
-    f_lmn and C_ln is compared.  The FP64 run is also timed (events on its stream)."""
-    L, M = a.lmax, a.nmax
-    f_s = d_f.cpu().numpy()
-    c_s = d_c.cpu().numpy().reshape(L, M)
-    d_f2 = torch.zeros_like(d_f)
-    d_c2 = torch.zeros_like(d_c)
-    d_k2 = torch.zeros_like(d_k)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    _lib.check(_lib.lib.catana_gpu_sfb_raw_dev(ctypes.c_void_p(d_pts.data_ptr()), ctypes.c_void_p(d_w.data_ptr()),
-                                               a.points, L, M, a.rmax, _lib.FORM_PLAIN | _lib.JL_POLY,
-                                               ctypes.c_void_p(d_k2.data_ptr()), ctypes.c_void_p(d_c2.data_ptr()),
-                                               ctypes.c_void_p(d_f2.data_ptr()), None, sp), "sfb_raw_dev poly")
-    e1.record()
-    torch.cuda.synchronize()
-    t_ref = e0.elapsed_time(e1) / 1e3
-    f_p = d_f2.cpu().numpy()
-    c_p = d_c2.cpu().numpy().reshape(L, M)
-    del d_f2, d_c2, d_k2
+def split_error_stats(f_s, c_s, f_p, c_p, L, M):
+    """Error of a split result (f_s, c_s) against an FP64 one (f_p, c_p), every mode."""
     fs = f_s[0::2] + 1j * f_s[1::2]
     fp = f_p[0::2] + 1j * f_p[1::2]
     rel = np.abs(c_s - c_p) / np.abs(c_p)
@@ -597,9 +584,6 @@ def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
     worst = np.argsort(rel, axis=None)[::-1][:8]
     med_l = np.median(c_p, axis=1)
     return {
-        "sample_points": a.points, "lmax": L, "nmax": M,
-        "reference": "FP64 plain GPU path, j_l from piecewise FP64 polynomials (CATANA_JL_POLY), same catalog",
-        "reference_seconds": t_ref, "reference_value": a.points * modes(L, M) / t_ref,
         "c_ln_rel_err_median": float(np.median(rel)), "c_ln_rel_err_p99": float(np.percentile(rel, 99)),
         "c_ln_rel_err_p999": float(np.percentile(rel, 99.9)), "c_ln_rel_err_max": float(rel.max()),
         "c_ln_modes": int(rel.size), "c_ln_modes_above_1e-6": int(over.sum()),
@@ -617,6 +601,49 @@ def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
                                           "l=%d" % (L - 1): float(rms_l[-1]), "max": float(rms_l.max()),
                                           "argmax_l": int(rms_l.argmax())},
     }
+
+
+def accuracy_full(torch, _lib, a, d_pts, d_w, d_k, d_c, d_f, sp):
+    """The split form's error on the whole catalog: d_f / d_c hold the split result of
+    the last timed step; the same catalog runs once more through the FP64 plain path
+    with j_l from the piecewise FP64 polynomials (CATANA_JL_POLY, pinned to the
+    oracle's exact j_l at 1e-10 of max|f| in tests/test_raw_fp64_gpu.py), and every
+    f_lmn and C_ln is compared.  The FP64 run is timed (events on its stream), and the
+    CATANA_SPLIT_ACCURATE variant of the split form is run, timed and compared too."""
+    L, M = a.lmax, a.nmax
+    f_s = d_f.cpu().numpy()
+    c_s = d_c.cpu().numpy().reshape(L, M)
+    d_f2 = torch.zeros_like(d_f)
+    d_c2 = torch.zeros_like(d_c)
+    d_k2 = torch.zeros_like(d_k)
+
+    def run(flags, reps=1):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            _lib.check(_lib.lib.catana_gpu_sfb_raw_dev(
+                ctypes.c_void_p(d_pts.data_ptr()), ctypes.c_void_p(d_w.data_ptr()), a.points, L, M, a.rmax, flags,
+                ctypes.c_void_p(d_k2.data_ptr()), ctypes.c_void_p(d_c2.data_ptr()), ctypes.c_void_p(d_f2.data_ptr()),
+                None, sp), "sfb_raw_dev")
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps, d_f2.cpu().numpy(), d_c2.cpu().numpy().reshape(L, M)
+
+    t_ref, f_p, c_p = run(_lib.FORM_PLAIN | _lib.JL_POLY)
+    out = {"sample_points": a.points, "lmax": L, "nmax": M,
+           "reference": "FP64 plain GPU path, j_l from piecewise FP64 polynomials (CATANA_JL_POLY), same catalog",
+           "reference_seconds": t_ref, "reference_value": a.points * modes(L, M) / t_ref}
+    out.update(split_error_stats(f_s, c_s, f_p, c_p, L, M))
+    run(_lib.FORM_SPLIT | _lib.SPLIT_ACCURATE)  # tables and workspace for this variant
+    t_acc, f_a, c_a = run(_lib.FORM_SPLIT | _lib.SPLIT_ACCURATE, reps=2)
+    acc = {"value": a.points * modes(L, M) / t_acc, "unit": UNIT, "ms_per_step": t_acc * 1e3,
+           "note": "CATANA_SPLIT_ACCURATE: Reinsch-modified Legendre rows for m < 128 (rows P_l and D_l at "
+                   "|cos theta|); same catalog, same FP64 reference"}
+    acc.update(split_error_stats(f_a, c_a, f_p, c_p, L, M))
+    out["split_accurate"] = acc
+    del d_f2, d_c2, d_k2
+    return out
 
 
 def workload_config(a):

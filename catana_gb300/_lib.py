@@ -29,6 +29,7 @@ OK, ERR_ARG, ERR_DOMAIN, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED = range(6)
 # flags
 JL_AUTO, JL_INTERP, JL_EXACT, JL_POLY = 0, 1, 2, 3
 FORM_PLAIN, FORM_SPLIT = 0, 4
+SPLIT_ACCURATE = 32
 HEALPIX_CONJ_FIX = 8
 BATCH_NO_GRAPH = 16
 

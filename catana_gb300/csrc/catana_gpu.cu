@@ -270,7 +270,8 @@ catana_status_t raw_device(DeviceContext *ctx, const double *pts_d, const double
             set_error("the split (tcgen05) form needs an sm_103 device");
             return CATANA_ERR_UNSUPPORTED;
         }
-        s = split_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, rmax, kln_d, facc, err_d, st);
+        s = split_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, rmax, kln_d, facc, err_d, st,
+                                 (flags & CATANA_SPLIT_ACCURATE) != 0);
     } else {
         s = fp64_raw_accumulate(ctx, pts_d, w_d, npoints, lmax, nmax, resolve_jl(flags, npoints), kln_d, facc,
                                 err_d, st);
@@ -385,6 +386,7 @@ catana_status_t batched_device(DeviceContext *ctx, const catana_catalog_t *cats,
                 in.kmax = C.kmax;
                 in.kln_dev = C.k_ln;
                 in.f_acc = facc[c];
+                in.accurate = (flags & CATANA_SPLIT_ACCURATE) != 0;
                 v.push_back(in);
             }
         }

@@ -141,6 +141,7 @@ struct SplitCatInput {
     double kmax = 0.0;            // > 0: keep only k_ln <= kmax
     double *kln_dev = nullptr;    // k_ln (lmax x nmax), already on the device
     double *f_acc = nullptr;      // packed complex f_lmn accumulator
+    bool accurate = false;        // CATANA_SPLIT_ACCURATE: Reinsch-modified Legendre rows (lmax <= 256)
 };
 // Split form over several catalogs: level-synchronous launches over all of them,
 // optionally captured as one CUDA graph.  `waves` = CTAs per SM each level's work
@@ -155,7 +156,7 @@ catana_status_t ingest_dev(DeviceContext *ctx, const void *rec_dev, int64_t n, c
 // Split (tensor-core) raw path (sfb_split.cu).
 catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
                                      int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
-                                     double *f_acc_dev, int *err_dev, cudaStream_t st);
+                                     double *f_acc_dev, int *err_dev, cudaStream_t st, bool accurate);
 
 // Stable radix sort of (key, index) pairs by the low key_bits bits (sort.cu).
 catana_status_t radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals, int64_t n,

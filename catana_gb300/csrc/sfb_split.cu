@@ -314,8 +314,9 @@ __device__ __forceinline__ float2 sum_once2(float2 rh, float2 rl, float2 p, floa
     return __fadd2_rn(s, __fadd2_rn(se, __ffma2_rn(rl, p, pl)));
 }
 
-template <bool EXT, bool FULLJ, int NST>
+template <bool EXT, bool FULLJ, int NST, bool RS>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
+    static_assert(!(EXT && RS), "the Reinsch-modified rows serve the plain range only");
     constexpr uint32_t STG = sm_stage(EXT);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         const float4 cb = 2 * t + 1 < mcount ? a.coef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
         s_coef[2 * t] = make_float4(ca.x, cb.x, ca.y, cb.y);
         s_coef[2 * t + 1] = make_float4(ca.z, cb.z, ca.w, cb.w);
-        if (!EXT) {
+        if (RS) {
             const float4 ra = a.rcoef[mb0 + 2 * t];
             const float4 rb = 2 * t + 1 < mcount ? a.rcoef[mb0 + 2 * t + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
             s_rcoef[2 * t] = make_float4(ra.x, rb.x, ra.y, rb.y);
@@ -407,9 +408,9 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
     const size_t set = (size_t)stride * cat.lrp;
-    // the rows this level writes: P_l (and, plain form, X_l)
-    float *__restrict__ st0 = cat.rows + (size_t)(EXT ? l % 3 : (l & 1)) * set;
-    float *__restrict__ xt0 = cat.rows + (size_t)(EXT ? 0 : 2 + (l & 1)) * set;
+    // the rows this level writes: P_l (and, Reinsch-modified rows, X_l)
+    float *__restrict__ st0 = cat.rows + (size_t)(RS ? (l & 1) : l % 3) * set;
+    float *__restrict__ xt0 = cat.rows + (size_t)(RS ? 2 + (l & 1) : 0) * set;
     const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
     unsigned long long *ex0 = nullptr;
     if (EXT) {
@@ -441,12 +442,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
     // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
     // and (extended range) the exponent words of both sets
-    // staged rows: P_{l-1} and (extended range) P_{l-2} or (plain form) X_{l-1}
-    const char *tm_r1 = cat.tmaps + 128 * (EXT ? (l + 2) % 3 : (l + 1) & 1);
-    const char *tm_r2 = cat.tmaps + 128 * (EXT ? (l + 1) % 3 : 2 + ((l + 1) & 1));
+    // staged rows: P_{l-1} and P_{l-2} (three-term rows) or X_{l-1} (Reinsch-modified rows)
+    const char *tm_r1 = cat.tmaps + 128 * (RS ? (l + 1) & 1 : (l + 2) % 3);
+    const char *tm_r2 = cat.tmaps + 128 * (RS ? 2 + ((l + 1) & 1) : (l + 1) % 3);
     const char *tm_e1 = cat.tmaps + 128 * (3 + (l + 2) % 3), *tm_e2 = cat.tmaps + 128 * (3 + (l + 1) % 3);
     const int nb1 = l > 0 ? (mcount + 31) >> 5 : 0;
-    const int nb2 = (max(0, min(mcount, EXT ? l - 1 - mb0 : l - mb0)) + 31) >> 5;
+    const int nb2 = (max(0, min(mcount, RS ? l - mb0 : l - 1 - mb0)) + 31) >> 5;
     const uint32_t stage_bytes =
         SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? 2u * (MBLK * 8) : 0u);
     if (tid == 0) {  // descriptors rewritten by the host between launches: read them afresh
@@ -586,8 +587,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                     2 * SM_STROW + q * 48);
             const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
-            // plain form: rows at |cos(theta)|, the factor (-1)^l of a southern point in its weight
-            const float wq = (!EXT && (l & 1) && (pt.u & 1ull)) ? -pt.w : pt.w;
+            // Reinsch-modified rows: at |cos(theta)|, the factor (-1)^l of a southern point in its weight
+            const float wq = (RS && (l & 1) && (pt.u & 1ull)) ? -pt.w : pt.w;
             // ---- J tile: n = 8 g .. 8 g + 7 ----
             if constexpr (FULLJ) {
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
@@ -802,7 +803,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                         {
                             const int m = mb0 + ml;
                             float2 P;
-                            if constexpr (!EXT) {
+                            if constexpr (RS) {
                                 // plain form: rows P_l and X_l at |cos(theta)|.  Columns m < MR_STD
                                 // take the Reinsch-modified step (X = D_l = P_l - rho_l P_{l-1}):
                                 //   D_l = c1_l D_{l-1} - A_l eps P_{l-1},  P_l = rho_l P_{l-1} + D_l,
@@ -1095,7 +1096,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
 // frame of the running 2-bit exponent (stored value P 2^100 2^(128 e), e raised when
 // the value drops below 2^-40, 0 below 2^-520), with the exponent word written too.
 __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const double *__restrict__ asect,
-                                 int64_t ntiles, int ext) {
+                                 int64_t ntiles, int mode) {
+    const bool ext = (mode == 2);
     const SplitCat c = cats[cat];
     const int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
     if (t >= ntiles) return;  // warp-uniform
@@ -1104,14 +1106,14 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
     const SplitPt &pt = c.pts[i];
     // sin(theta): stored (extended range), or from eps = 1 - |cos(theta)| as sqrt(eps (2 - eps))
     const double sv = (double)pt.s_hi + (double)pt.s_lo;
-    const double s = ext ? sv : sqrt(sv * (2.0 - sv));
+    const double s = mode == 1 ? sqrt(sv * (2.0 - sv)) : sv;
     const size_t set = (size_t)c.stride * c.lrp;
     float *rt = c.rows + 2 * i;  // this point in the pair-interleaved rows
     double P = (double)P00_SCALED;
     unsigned e = 0;
     for (int l = 1; l < lmax; ++l) {
         P = asect[l] * s * P;
-        const int k = ext ? (l + 2) % 3 : (l + 1) & 1;  // the set of P_{l-1}
+        const int k = mode == 1 ? (l + 1) & 1 : (l + 2) % 3;  // the set of P_{l-1}
         float v;
         if (ext) {
             double f = P;
@@ -1497,6 +1499,8 @@ std::atomic<uint64_t> g_split_stall_ns{0};
 
 catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_in, bool use_graph,
                           double waves, int *err_dev, cudaStream_t st) {
+    // every catalog of a call carries the same flags
+    const bool accurate = !cats_in.empty() && cats_in.front().accurate;
     std::vector<CatPlan> cats;
     for (auto &c : cats_in) {
         if (c.lmax > SPLIT_LMAX_EXT || c.nmax > SPLIT_NMAX) {
@@ -1516,9 +1520,11 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
     // the test hook (catana_gpu_test_split_stall) arms one run
     const uint64_t stall_ns = g_split_stall_ns.exchange(0);
     if (!ctx->attr_split) {
-        void (*const kerns[])(SplitArgs) = {k_split_l<false, true, 2>, k_split_l<false, false, 2>,
-                                            k_split_l<false, true, 3>, k_split_l<false, false, 3>,
-                                            k_split_l<true, true, 2>,  k_split_l<true, false, 2>};
+        void (*const kerns[])(SplitArgs) = {
+            k_split_l<false, true, 2, false>, k_split_l<false, false, 2, false>, k_split_l<false, true, 3, false>,
+            k_split_l<false, false, 3, false>, k_split_l<false, true, 2, true>,  k_split_l<false, false, 2, true>,
+            k_split_l<false, true, 3, true>,  k_split_l<false, false, 3, true>,  k_split_l<true, true, 2, false>,
+            k_split_l<true, false, 2, false>};
         for (auto kf : kerns)
             CG_CUDA_TRY(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
         ctx->attr_split = true;
@@ -1612,7 +1618,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
         // row sets: plain form P_l, X_l by the parity of l (X = D or P_{l-1}); extended range
         // P_l, P_{l-1}, P_{l-2} rotating
-        const int nsets = ext ? 3 : 4;
+        const bool rs = accurate && !ext;  // Reinsch-modified rows (CATANA_SPLIT_ACCURATE)
+        const int nsets = rs ? 4 : 3;
         // three stages (tiles staged two ahead) where shared memory allows: plain rows and a
         // table of at most ~750 intervals; otherwise two
         const int nst = (!ext && smem_bytes(false, 3, nint) <= SMEM_LIMIT) ? 3 : 2;
@@ -1620,9 +1627,13 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         // kernel per level: extended-range rows above lmax 256; the full-J layout when every
         // item of the level has 128 radial orders in its half
         auto kern_for = [&](bool full) {
-            if (ext) return full ? k_split_l<true, true, 2> : k_split_l<true, false, 2>;
-            if (nst == 3) return full ? k_split_l<false, true, 3> : k_split_l<false, false, 3>;
-            return full ? k_split_l<false, true, 2> : k_split_l<false, false, 2>;
+            if (ext) return full ? k_split_l<true, true, 2, false> : k_split_l<true, false, 2, false>;
+            if (rs) {
+                if (nst == 3) return full ? k_split_l<false, true, 3, true> : k_split_l<false, false, 3, true>;
+                return full ? k_split_l<false, true, 2, true> : k_split_l<false, false, 2, true>;
+            }
+            if (nst == 3) return full ? k_split_l<false, true, 3, false> : k_split_l<false, false, 3, false>;
+            return full ? k_split_l<false, true, 2, false> : k_split_l<false, false, 2, false>;
         };
         // workspace: per catalog records + rows (+ exponents); sort scratch sized for the largest
         int64_t smax = 0;
@@ -1661,10 +1672,10 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             const int64_t npad = P.ntiles * KT;
             if (P.in.pts32)
                 k_split_prep<float><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts32, P.in.w32, perm, n, npad, spts,
-                                                                         err_dev, ext ? 0 : 1);
+                                                                         err_dev, rs ? 1 : 0);
             else
                 k_split_prep<double><<<ceil_div(npad, 256), 256, 0, st>>>(P.in.pts, P.in.w, perm, n, npad, spts,
-                                                                          err_dev, ext ? 0 : 1);
+                                                                          err_dev, rs ? 1 : 0);
             count_launch();
             CG_CUDA_TRY(cudaGetLastError());
         }
@@ -1946,7 +1957,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 k_split_sectoral<<<ceil_div(nt, 8), 256, 0, st>>>(reinterpret_cast<const SplitCat *>(pd + o_cats),
                                                                   c - c0, cats[c].in.lmax,
                                                                   reinterpret_cast<const double *>(pd + o_as), nt,
-                                                                  ext ? 1 : 0);
+                                                                  ext ? 2 : (rs ? 1 : 0));
                 count_launch();
             }
             CG_CUDA_TRY(cudaGetLastError());
@@ -2001,7 +2012,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
 
 catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_dev, const double *weights_dev,
                                      int64_t npoints, int lmax, int nmax, double rmax, const double *kln_dev,
-                                     double *f_acc_dev, int *err_dev, cudaStream_t st) {
+                                     double *f_acc_dev, int *err_dev, cudaStream_t st, bool accurate) {
     if (npoints == 0 || lmax == 0 || nmax == 0) return CATANA_OK;
     // chunks whose Legendre rows stay under 16 GB; they share the accumulator, so
     // split_run places each in its own group and runs the groups one after another
@@ -2018,6 +2029,7 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
         in.kmax = 0.0;
         in.kln_dev = const_cast<double *>(kln_dev);
         in.f_acc = f_acc_dev;
+        in.accurate = accurate;
         v.push_back(in);
     }
     return split_run(ctx, v, false, 1.0, err_dev, st);

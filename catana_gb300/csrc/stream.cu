@@ -143,6 +143,7 @@ catana_status_t accum_add(Accum *A, const T *points, const T *weights, int64_t n
             in.max_w = max_w;
             in.kln_dev = A->kln.as<double>();
             in.f_acc = A->facc.as<double>();
+            in.accurate = (A->flags & CATANA_SPLIT_ACCURATE) != 0;
             v.push_back(in);
         }
         s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);
@@ -227,6 +228,7 @@ catana_status_t accum_add_records(Accum *A, const void *records, int64_t n, cons
                 in.rmax = A->rmax;
                 in.kln_dev = A->kln.as<double>();
                 in.f_acc = A->facc.as<double>();
+                in.accurate = (A->flags & CATANA_SPLIT_ACCURATE) != 0;
                 v.push_back(in);
             }
             s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);

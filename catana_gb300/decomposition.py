@@ -10,7 +10,9 @@ HEALPix method (py_decomposition.cpp:135-153, sfb_decomposition.cpp:22-26).
 Keyword extensions (absent in the reference, defaults reproduce it):
   weights=None         per-point weights; f is normalised by V/sum(w)
   precision='plain'    'plain': FP64 on CUDA cores (the drop-in);
-                       'split': tcgen05 tensor cores, 3-term FP16 hi+lo products
+                       'split': tcgen05 tensor cores, 3-term FP16 hi+lo products;
+                       'split_accurate': the same with Reinsch-modified Legendre
+                       rows (lmax <= 256): half the f_lmn error at high l, ~12% slower
   interpolation='auto' 'auto' (interpolated iff N > 1000, the reference's rule),
                        'on' (linear table), 'off' (exact j_l) or 'poly' (piecewise
                        FP64 polynomials, as accurate as 'off' at the cost of 'on';
@@ -28,7 +30,8 @@ from . import _lib
 from .basictypes import PixelizedPointContainer, PointContainer
 
 _INTERP = {"auto": _lib.JL_AUTO, "on": _lib.JL_INTERP, "off": _lib.JL_EXACT, "poly": _lib.JL_POLY}
-_FORM = {"plain": _lib.FORM_PLAIN, "split": _lib.FORM_SPLIT}
+_FORM = {"plain": _lib.FORM_PLAIN, "split": _lib.FORM_SPLIT,
+         "split_accurate": _lib.FORM_SPLIT | _lib.SPLIT_ACCURATE}
 
 
 class KClkk(object):

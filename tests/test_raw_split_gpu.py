@@ -1,6 +1,9 @@
 """The split-precision tensor-core form (tcgen05, 3-term FP16 hi+lo products, FP32
 accumulation folded per 32-point tile, FP32 partial per work item, FP64 across items)
-against the FP64 oracle with exact j_l.
+against the FP64 oracle with exact j_l (or, at sizes the oracle does not finish in seconds,
+the FP64 GPU path with j_l from its FP64 polynomials, itself pinned to the oracle).
+Both split variants: the default three-term Legendre rows and the Reinsch-modified
+rows of CATANA_SPLIT_ACCURATE.
 
 Error measures (measured values are ~2e-7 median, ~6e-7 p99 on 100k points):
   C_ln   median relative error <= 5e-7 and 99th percentile <= 2e-6; every entry
@@ -40,6 +43,10 @@ def _check(res, f, c, tag):
     assert typ.max() <= 1e-5
 
 
+FORMS = ["split", "split_accurate"]
+
+
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("n,lmax,nmax,weighted", [
     (3000, 8, 8, False),
     (5000, 33, 20, True),
@@ -47,17 +54,18 @@ def _check(res, f, c, tag):
     (20000, 40, 100, False),  # several tiles per CTA: per-tile folds
     (3000, 24, 200, True),    # nmax > 128: two radial halves
 ])
-def test_split_vs_oracle(sm103, n, lmax, nmax, weighted):
+def test_split_vs_oracle(sm103, n, lmax, nmax, weighted, form):
     pts = uniform_ball(n, 1000.0, seed=100 + n)
     w = np.random.default_rng(n).uniform(0.5, 1.5, n) if weighted else None
     res = catana.sfb_decomposition(catana.PointContainer(pts), lmax, nmax, 1000.0, True, False,
-                                   weights=w, precision="split")
+                                   weights=w, precision=form)
     k, c, f = O.sfb_raw(pts, lmax, nmax, 1000.0, interpolated=False, weights=w)
     assert np.array_equal(res.k_ln, k)
-    _check(res, f, c, "split n=%d lmax=%d nmax=%d" % (n, lmax, nmax))
+    _check(res, f, c, "%s n=%d lmax=%d nmax=%d" % (form, n, lmax, nmax))
 
 
-def test_split_full_shape_vs_fp64_gpu(sm103):
+@pytest.mark.parametrize("form", FORMS)
+def test_split_full_shape_vs_fp64_gpu(sm103, form):
     """lmax=256, nmax=128 (the precision form's headline shape) on a 20k-point
     subsample of the uniform ball with weights U[0.5,1.5]: split vs the plain FP64
     GPU path in exact-j_l mode (itself pinned to the oracle)."""
@@ -65,12 +73,13 @@ def test_split_full_shape_vs_fp64_gpu(sm103):
     pts = uniform_ball(n, 1000.0, seed=2)
     w = np.random.default_rng(2).uniform(0.5, 1.5, n)
     pc = catana.PointContainer(pts)
-    rs = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, precision="split")
-    rp = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, interpolation="off")
-    _check(rs, rp.f_lmn, rp.c_ln, "split lmax=256 nmax=128 n=20000")
+    rs = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, precision=form)
+    rp = catana.sfb_decomposition(pc, 256, 128, 1000.0, True, False, weights=w, interpolation="poly")
+    _check(rs, rp.f_lmn, rp.c_ln, "%s lmax=256 nmax=128 n=20000" % form)
 
 
-def test_split_long_items_vs_fp64_gpu(sm103):
+@pytest.mark.parametrize("form", FORMS)
+def test_split_long_items_vs_fp64_gpu(sm103, form):
     """2M points: about 400 tiles per work item, so each item folds into its TMEM sum
     and flushes it into its running FP32 partial several times (read-modify-write of
     the partial) before the last flush; split vs the plain FP64 GPU path with exact j_l
@@ -81,9 +90,9 @@ def test_split_long_items_vs_fp64_gpu(sm103):
     pts = uniform_ball(n, 1000.0, seed=77)
     w = np.random.default_rng(77).uniform(0.5, 1.5, n)
     pc = catana.PointContainer(pts)
-    rs = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, precision="split")
-    rp = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, interpolation="off")
-    _check(rs, rp.f_lmn, rp.c_ln, "split lmax=64 nmax=32 n=2M")
+    rs = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, precision=form)
+    rp = catana.sfb_decomposition(pc, 64, 32, 1000.0, True, False, weights=w, interpolation="poly")
+    _check(rs, rp.f_lmn, rp.c_ln, "%s lmax=64 nmax=32 n=2M" % form)
 
 
 def test_split_multi_chunk_linearity(sm103):
