@@ -424,9 +424,11 @@ def streamed_workload(torch, _lib, catana, chunks=2, chunk=8_000_000, L=512, M=2
     decomposition) + finish (normalisation, C_ln, copies back)."""
     rng = np.random.default_rng(seed)
     host = []
-    for _ in range(chunks):
-        t = torch.empty((chunk, 3), dtype=torch.float32, pin_memory=True)
-        t.numpy()[:] = survey_chunk(rng, chunk)
+    total = min(chunks * chunk, 100_000_000)  # the survey: 100M points, the last chunk shorter
+    for c in range(chunks):
+        n_c = min(chunk, total - c * chunk)
+        t = torch.empty((n_c, 3), dtype=torch.float32, pin_memory=True)
+        t.numpy()[:] = survey_chunk(rng, n_c)
         host.append(t)
     warm = survey_chunk(rng, 50000)
     with catana.SFBAccumulator(L, M, 1500.0, precision="split") as acc:  # builds the j_l tables once
@@ -443,8 +445,8 @@ def streamed_workload(torch, _lib, catana, chunks=2, chunk=8_000_000, L=512, M=2
     _lib.lib.catana_gpu_profile_enable(0)
     kms, kn, kfl = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_double()
     _lib.check(_lib.lib.catana_gpu_profile_report(ctypes.byref(kms), ctypes.byref(kn), ctypes.byref(kfl)))
-    pm = float(chunks * chunk) * modes(L, M)
-    out = {"value": pm / dt, "unit": UNIT, "seconds": dt, "points": chunks * chunk, "chunk": chunk, "lmax": L,
+    pm = float(total) * modes(L, M)
+    out = {"value": pm / dt, "unit": UNIT, "seconds": dt, "points": total, "chunks": chunks, "chunk": chunk, "lmax": L,
            "nmax": M, "input": "float32 (r, theta, phi), pinned host memory",
            "contraction_kernel_s": kms.value / 1e3, "contraction_tflops_algorithmic": kfl.value / (kms.value / 1e3) / 1e12,
            "c_ln_finite": bool(np.isfinite(res.c_ln).all())}
