@@ -29,9 +29,12 @@
 //     (staged into shared memory one tile ahead by TMA), with the recurrence
 //     coefficients and x = cos(theta), s = sin(theta) as float-float pairs; the rows
 //     are stored scaled by 2^100 so that sectoral seeds down to 2^-226 stay
-//     representable (enough for lmax <= 256); the m = 0 step is rounded once
-//     (step_once), so Y_l0 carries no mean error over the sphere through which a
-//     catalog's monopole could leak into l > 0;
+//     representable (enough for lmax <= 256; above, each value carries a 2-bit exponent);
+//     the m = 0 step is rounded once (step_once), so Y_l0 carries no mean error over the
+//     sphere through which a catalog's monopole could leak into l > 0.  With
+//     CATANA_SPLIT_ACCURATE the columns m < 128 follow the Reinsch-modified recurrence
+//     at |cos(theta)| instead (rows P_l and D_l = P_l - rho_l P_{l-1}), whose rounding
+//     does not build up near the poles;
 //   * the sectoral seeds stay FP64: before the level loop, k_split_sectoral advances
 //     every point's P_ll = -sqrt((2l+1)/(2l)) s P_{l-1,l-1} in FP64 from the FP32
 //     value of P_00 and stores each level's P_ll, rounded once, in slot m = l of the
@@ -82,7 +85,7 @@ constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 
 constexpr int SPLIT_LMAX_EXT = 512; // with the 2-bit row exponents (extended range)
 constexpr int SPLIT_NMAX = 256;     // two 128-lane halves (separate work items)
 constexpr int NHALF = 128;          // radial orders per work item (accumulator lanes)
-constexpr int MR_STD = 128;         // plain form: columns m >= MR_STD keep the three-term step
+constexpr int MR_STD = 128;         // Reinsch-modified rows: columns m >= MR_STD keep the three-term step
 constexpr uint64_t WAIT_NS = 1000000000ull;  // drains of in-flight copies and MMAs before exit (1 s)
 
 // shared-memory map (bytes, from a 1024-aligned base)
@@ -92,23 +95,37 @@ constexpr uint32_t SM_BUF = 2 * SM_J + 2 * SM_Y;
 constexpr uint32_t OFF_ST = 2 * SM_BUF;                // staged tiles: NST stages (2 or 3)
 constexpr uint32_t SM_STROW = MBLK * KT * 4;           // one row set (MBLK m x 32 points) = 16 KB
 constexpr uint32_t SM_STPTS = KT * 48;                 // the tile's 32 SplitPt records
-constexpr uint32_t SM_STEXP = 2 * MBLK * 8;            // row exponent words of P_{l-1}, P_{l-2} (extended range)
-// one stage: P_{l-1}, P_{l-2}, the points (and, extended range, the exponent words)
-__host__ __device__ constexpr uint32_t sm_stage(bool ext) { return 2 * SM_STROW + SM_STPTS + (ext ? SM_STEXP : 0u); }
+constexpr uint32_t SM_STEXP = MBLK * 8;                // row exponent words of one row set (extended range)
+// one stage: P_{l-1}, P_{l-2} (Reinsch-modified rows: X_{l-1}), the points and, extended
+// range, the exponent words of both row sets (Reinsch-modified rows: one word serves
+// P_{l-1} and X_{l-1})
+__host__ __device__ constexpr uint32_t sm_stage(bool ext, bool rs) {
+    return 2 * SM_STROW + SM_STPTS + (ext ? (rs ? 1u : 2u) * SM_STEXP : 0u);
+}
 // after the stages: per n pair (kz_hi, kz_lo) x 2; J scale 2^s_ln per n; readout 2^-s_ln 2^-12 per
-// n; recurrence coefficients of the m pairs; per operand warp the Taylor coefficients of its 8 J
-// rows; last, the j_l table of the launch (its interval count sets the dynamic size)
-__host__ __device__ constexpr uint32_t off_kz(bool ext, int nst) { return OFF_ST + (uint32_t)nst * sm_stage(ext); }
-__host__ __device__ constexpr uint32_t off_js(bool ext, int nst) { return off_kz(ext, nst) + NHALF * 8; }
-__host__ __device__ constexpr uint32_t off_inv(bool ext, int nst) { return off_js(ext, nst) + NHALF * 4; }
-__host__ __device__ constexpr uint32_t off_coef(bool ext, int nst) { return off_inv(ext, nst) + NHALF * 4; }
-__host__ __device__ constexpr uint32_t off_rcoef(bool ext, int nst) { return off_coef(ext, nst) + MBLK * 16; }
-__host__ __device__ constexpr uint32_t off_jt(bool ext, int nst) { return off_rcoef(ext, nst) + (ext ? 0u : MBLK * 16); }
-__host__ __device__ constexpr uint32_t off_tab(bool ext, int nst) { return off_jt(ext, nst) + (NTHR / 32) * 32 * 4; }
+// n; recurrence coefficients of the m pairs (and of the Reinsch-modified step); per operand warp
+// the Taylor coefficients of its 8 J rows; last, the j_l table of the launch (its interval count
+// sets the dynamic size)
+__host__ __device__ constexpr uint32_t off_kz(bool ext, bool rs, int nst) {
+    return OFF_ST + (uint32_t)nst * sm_stage(ext, rs);
+}
+__host__ __device__ constexpr uint32_t off_js(bool ext, bool rs, int nst) { return off_kz(ext, rs, nst) + NHALF * 8; }
+__host__ __device__ constexpr uint32_t off_inv(bool ext, bool rs, int nst) { return off_js(ext, rs, nst) + NHALF * 4; }
+__host__ __device__ constexpr uint32_t off_coef(bool ext, bool rs, int nst) { return off_inv(ext, rs, nst) + NHALF * 4; }
+__host__ __device__ constexpr uint32_t off_rcoef(bool ext, bool rs, int nst) { return off_coef(ext, rs, nst) + MBLK * 16; }
+__host__ __device__ constexpr uint32_t off_jt(bool ext, bool rs, int nst) {
+    return off_rcoef(ext, rs, nst) + (ext && !rs ? 0u : MBLK * 16);
+}
+__host__ __device__ constexpr uint32_t off_tab(bool ext, bool rs, int nst) {
+    return off_jt(ext, rs, nst) + (NTHR / 32) * 32 * 4;
+}
 // dynamic shared memory of a launch (+ 1024 B of alignment slack)
-constexpr uint32_t smem_bytes(bool ext, int nst, int nint) { return off_tab(ext, nst) + (uint32_t)nint * 32 + 1024; }
+constexpr uint32_t smem_bytes(bool ext, bool rs, int nst, int nint) {
+    return off_tab(ext, rs, nst) + (uint32_t)nint * 32 + 1024;
+}
 constexpr uint32_t SMEM_LIMIT = 232448 - 1024;  // per block, leaving room for the static part
-static_assert(smem_bytes(true, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
+static_assert(smem_bytes(true, false, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
+static_assert(smem_bytes(true, true, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
 // J of a tile comes from a cubic Taylor expansion about its record-16 radius when
 // k_max max|r - r_c| <= JT_TAU: the omitted terms are below JT_TAU^4 / 24 ~ 7e-9 of j_l's
 // envelope (the interpolant's derivatives are bounded by it)
@@ -123,8 +140,8 @@ constexpr float Y_SCALE = 4096.0f;                    // 2^12
 // Per-point operand inputs of the split form (48 bytes, radius-sorted order).
 struct SplitPt {
     float r_hi, r_lo, w;        // radius (float-float), weight
-    float x_hi, x_lo;           // cos(theta), plain form |cos(theta)| (float-float)
-    float s_hi, s_lo;           // sin(theta), plain form 1 - |cos(theta)| (float-float)
+    float x_hi, x_lo;           // cos(theta); Reinsch-modified rows: |cos(theta)| (float-float)
+    float s_hi, s_lo;           // sin(theta); Reinsch-modified rows: 1 - |cos(theta)| (float-float)
     float cphi, sphi;           // e^{i phi}
     float dr;                   // r - r of the tile's record 16; record 16 itself: max |dr| of the tile
     unsigned long long u;       // phi / 2pi as a 64-bit fraction of a turn
@@ -135,18 +152,19 @@ static_assert(sizeof(SplitPt) == 48, "SplitPt layout");
 struct SplitCat {
     const SplitPt *pts;     // radius-sorted point records, padded to whole tiles
     float *rows;            // Legendre row sets with m pairs interleaved per point: value (m, i) of set k
-                            // at rows + k * stride * lrp + 2 stride (m / 2) + 2 i + m % 2.  Plain form:
-                            // sets 0, 1 = P_l by the parity of l, sets 2, 3 = X_l likewise; extended
-                            // range: sets l % 3 = P_l
+                            // at rows + k * stride * lrp + 2 stride (m / 2) + 2 i + m % 2.
+                            // Reinsch-modified rows: sets 0, 1 = P_l by the parity of l, sets 2, 3 =
+                            // X_l likewise; three-term rows: sets l % 3 = P_l
     int64_t n;              // points
     int stride;             // row stride (multiple of 32, >= n)
     int lrows;              // rows per set (the catalog's lmax)
     int lrp;                // lrows rounded up to even (m pairs per tile block: lrp / 2)
     int kzw;                // row width of kz (the catalog's nmax)
     int epitch;             // exponent words per tile (lrows rounded up to even)
-    unsigned long long *rexp;  // extended range: three exponent sets [tile][lrows], set k at rexp + k * eset
+    unsigned long long *rexp;  // extended range: exponent sets [tile][lrows], set k at rexp + k * eset (three-term
+                               // rows: three rotating with l % 3; Reinsch-modified rows: 0, 1 by the parity of l)
     int64_t eset;           // words per exponent set
-    const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..2, then exponent words of sets 0..2
+    const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..3, exponent words of sets 0..2 at 4..6
     const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
 };
@@ -170,21 +188,8 @@ struct SplitArgs {
     int stall;               // test hook: withhold the first operand hand-off of every item
 };
 
-__device__ __forceinline__ void store_split8(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, const float (&v)[8]) {
-    uint32_t h[4], o[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        __half2 hh = __floats2half2_rn(v[2 * k], v[2 * k + 1]);
-        float2 hf = __half22float2(hh);
-        __half2 ll = __floats2half2_rn(v[2 * k] - hf.x, v[2 * k + 1] - hf.y);
-        h[k] = *reinterpret_cast<uint32_t *>(&hh);
-        o[k] = *reinterpret_cast<uint32_t *>(&ll);
-    }
-    *reinterpret_cast<uint4 *>(hi_base + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
-}
-
-// Same for four value pairs (columns 2k, 2k+1 from v[k]) with packed FP32 arithmetic.
+// FP16 hi + lo halves of eight values, value pairs (columns 2k, 2k+1) from v[k], with packed
+// FP32 arithmetic: hi = v rounded to FP16, lo = v - hi rounded to FP16; 16 bytes of each half.
 __device__ __forceinline__ void store_split8p(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, float2 v0, float2 v1,
                                               float2 v2, float2 v3) {
     const float2 v[4] = {v0, v1, v2, v3};
@@ -316,8 +321,7 @@ __device__ __forceinline__ float2 sum_once2(float2 rh, float2 rl, float2 p, floa
 
 template <bool EXT, bool FULLJ, int NST, bool RS>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
-    static_assert(!(EXT && RS), "the Reinsch-modified rows serve the plain range only");
-    constexpr uint32_t STG = sm_stage(EXT);
+    constexpr uint32_t STG = sm_stage(EXT, RS);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     __shared__ uint64_t mbar[2];  // MMA completion per operand buffer
@@ -342,12 +346,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     while ((int)half_cols < ncols_pad) half_cols <<= 1;
     const uint32_t tcols = 2 * half_cols;  // D_tile at column 0, D_acc at column half_cols
 
-    float4 *s_tab = reinterpret_cast<float4 *>(sm + off_tab(EXT, NST));
-    float4 *s_kzp = reinterpret_cast<float4 *>(sm + off_kz(EXT, NST));  // n pair j: (hi n, hi n+1, lo n, lo n+1)
-    float *s_js = reinterpret_cast<float *>(sm + off_js(EXT, NST));
-    float *s_inv = reinterpret_cast<float *>(sm + off_inv(EXT, NST));
-    float4 *s_coef = reinterpret_cast<float4 *>(sm + off_coef(EXT, NST));  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
-    float4 *s_rcoef = reinterpret_cast<float4 *>(sm + off_rcoef(EXT, NST));  // m pair j: (c1_hi x2, c1_lo x2), (rho_hi x2, rho_lo x2)
+    float4 *s_tab = reinterpret_cast<float4 *>(sm + off_tab(EXT, RS, NST));
+    float4 *s_kzp = reinterpret_cast<float4 *>(sm + off_kz(EXT, RS, NST));  // n pair j: (hi n, hi n+1, lo n, lo n+1)
+    float *s_js = reinterpret_cast<float *>(sm + off_js(EXT, RS, NST));
+    float *s_inv = reinterpret_cast<float *>(sm + off_inv(EXT, RS, NST));
+    float4 *s_coef = reinterpret_cast<float4 *>(sm + off_coef(EXT, RS, NST));  // m pair j: (A_hi x2, A_lo x2), (B_hi x2, B_lo x2)
+    float4 *s_rcoef = reinterpret_cast<float4 *>(sm + off_rcoef(EXT, RS, NST));  // m pair j: (c1_hi x2, c1_lo x2), (rho_hi x2, rho_lo x2)
     const float4 *kz_row = cat.kz + (size_t)l * cat.kzw + nh0;
     const float kmax_j = nmax > 0 ? kz_row[nmax - 1].x : 0.f;  // largest k_ln / H of this half (k grows with n)
     for (int t = tid; t < 2 * a.nint; t += NTOT) s_tab[t] = a.tab[t];
@@ -411,13 +415,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // the rows this level writes: P_l (and, Reinsch-modified rows, X_l)
     float *__restrict__ st0 = cat.rows + (size_t)(RS ? (l & 1) : l % 3) * set;
     float *__restrict__ xt0 = cat.rows + (size_t)(RS ? 2 + (l & 1) : 0) * set;
-    const unsigned long long *ex1 = nullptr, *ex2 = nullptr;
+    // extended range: the exponent words this level writes (three-term rows: sets rotating
+    // with l % 3 like the rows; Reinsch-modified rows: by the parity of l, one word for P_l and X_l)
     unsigned long long *ex0 = nullptr;
-    if (EXT) {
-        ex1 = cat.rexp + (size_t)((l + 2) % 3) * cat.eset;
-        ex2 = cat.rexp + (size_t)((l + 1) % 3) * cat.eset;
-        ex0 = cat.rexp + (size_t)(l % 3) * cat.eset;
-    }
+    if (EXT) ex0 = cat.rexp + (size_t)(RS ? (l & 1) : l % 3) * cat.eset;
     float *__restrict__ partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
@@ -441,21 +442,23 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // records (one bulk copy), the rows P_{l-1}(m) and P_{l-2}(m) of this block's m in
     // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
     // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
-    // and (extended range) the exponent words of both sets
-    // staged rows: P_{l-1} and P_{l-2} (three-term rows) or X_{l-1} (Reinsch-modified rows)
+    // and (extended range) the exponent words of both sets (Reinsch-modified rows: of level l-1)
+    // staged rows: P_{l-1} and P_{l-2} (three-term rows) or X_{l-1} (Reinsch-modified rows);
+    // descriptors 0..3 are the row sets, 4..6 the exponent sets
     const char *tm_r1 = cat.tmaps + 128 * (RS ? (l + 1) & 1 : (l + 2) % 3);
     const char *tm_r2 = cat.tmaps + 128 * (RS ? 2 + ((l + 1) & 1) : (l + 1) % 3);
-    const char *tm_e1 = cat.tmaps + 128 * (3 + (l + 2) % 3), *tm_e2 = cat.tmaps + 128 * (3 + (l + 1) % 3);
+    const char *tm_e1 = cat.tmaps + 128 * (4 + (RS ? (l + 1) & 1 : (l + 2) % 3));
+    const char *tm_e2 = cat.tmaps + 128 * (4 + (l + 1) % 3);
     const int nb1 = l > 0 ? (mcount + 31) >> 5 : 0;
     const int nb2 = (max(0, min(mcount, RS ? l - mb0 : l - 1 - mb0)) + 31) >> 5;
     const uint32_t stage_bytes =
-        SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? 2u * (MBLK * 8) : 0u);
+        SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? (RS ? 1u : 2u) * SM_STEXP : 0u);
     if (tid == 0) {  // descriptors rewritten by the host between launches: read them afresh
         tc05::tmap_acquire(tm_r1);
         tc05::tmap_acquire(tm_r2);
         if (EXT) {
             tc05::tmap_acquire(tm_e1);
-            tc05::tmap_acquire(tm_e2);
+            if (!RS) tc05::tmap_acquire(tm_e2);
         }
     }
     auto prefetch = [&](int64_t j) {
@@ -474,7 +477,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             tc05::tma_load_2d(stg + SM_STROW + k * 4096, tm_r2, (int)(2 * KT * t), (mb0 >> 1) + 16 * k, &sbar[sidx]);
         if (EXT && l > 0) {
             tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
-            tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + MBLK * 8, tm_e2, mb0, (int)t, &sbar[sidx]);
+            if (!RS) tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + SM_STEXP, tm_e2, mb0, (int)t, &sbar[sidx]);
         }
     };
     // the load of tile t0 + j is the (j / NST)-th completion of its stage's barrier
@@ -601,7 +604,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                     // J(n, q) = w_q sum_j c'_j dr_q^j about the tile's record-16 radius r_c:
                     // c'_j = 2^s_n k_n^j p^(j)(u0_n) / j!, p the interval polynomial, u0_n the
                     // offset of z_n = k_n r_c in its interval (float-float product)
-                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, NST)) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + 32 * g;
                     __syncwarp();
                     if (lane < 8) {
                         const int n = n0 + lane;
@@ -691,7 +694,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
-                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, NST)) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + 32 * g;
                     __syncwarp();
                     if (lane < 2 * (jp1 - jp0)) {  // rows past the count have k = 0, J scale 0: zero coefficients
                         const int n = 2 * jp0 + lane;
@@ -778,7 +781,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             }
             // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
             if (mlo < mhi) {
-                // x = cos(theta) (plain form: |cos(theta)|) and, plain form, eps = 1 - |cos(theta)|
+                // x = cos(theta) (Reinsch-modified rows: |cos(theta)|) and eps = 1 - |cos(theta)|
                 const float xh = pt.x_hi, xl = pt.x_lo, eh = pt.s_hi, el = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
                 // e^{i m phi} for the pair (m, m+1), times the readout factor 2^-88 of the scaled
                 // rows (exact): seed m, one rotation by e^{i phi}; pairs then advance by
@@ -804,7 +807,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                             const int m = mb0 + ml;
                             float2 P;
                             if constexpr (RS) {
-                                // plain form: rows P_l and X_l at |cos(theta)|.  Columns m < MR_STD
+                                // rows P_l and X_l at |cos(theta)|.  Columns m < MR_STD
                                 // take the Reinsch-modified step (X = D_l = P_l - rho_l P_{l-1}):
                                 //   D_l = c1_l D_{l-1} - A_l eps P_{l-1},  P_l = rho_l P_{l-1} + D_l,
                                 // in which near the poles (eps -> 0) D is small and the rounding of
@@ -816,6 +819,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                     const float2 p1 = reinterpret_cast<const float2 *>(stg1)[(ml >> 1) * KT + q];
                                     const float2 x1 = reinterpret_cast<const float2 *>(stg2)[(ml >> 1) * KT + q];
                                     const float4 ca = s_coef[ml];
+                                    // extended range: P_{l-1} and X_{l-1} share one exponent per (point, m)
+                                    unsigned ea = 0, eb = 0;
+                                    if (EXT) {
+                                        ea = ebits(stge1[ml], q);
+                                        eb = ebits(stge1[ml + 1], q);
+                                    }
                                     float2 Xn;
                                     if (m >= MR_STD) {
                                         const float4 cb = s_coef[ml + 1];
@@ -838,9 +847,35 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                             P = __ffma2_rn(make_float2(rb.x, rb.y), p1,
                                                            __ffma2_rn(make_float2(rb.z, rb.w), p1, Xn));
                                     }
+                                    if (EXT) {  // renormalise P_l and X_l together once P_l grew past 2^40 while e > 0
+                                        if (ea > 0 && fabsf(P.x) > 0x1p40f) {
+                                            P.x = P.x * 0x1p-64f * 0x1p-64f;
+                                            Xn.x = Xn.x * 0x1p-64f * 0x1p-64f;
+                                            --ea;
+                                        }
+                                        if (eb > 0 && fabsf(P.y) > 0x1p40f) {
+                                            P.y = P.y * 0x1p-64f * 0x1p-64f;
+                                            Xn.y = Xn.y * 0x1p-64f * 0x1p-64f;
+                                            --eb;
+                                        }
+                                    }
                                     if (wrows) {
                                         *reinterpret_cast<float2 *>(rowp) = P;
                                         *reinterpret_cast<float2 *>(xrowp) = Xn;
+                                    }
+                                    if (EXT && wrows) {
+                                        const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
+                                        const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
+                                        const unsigned b0 = __ballot_sync(0xffffffffu, eb & 1u);
+                                        const unsigned b1 = __ballot_sync(0xffffffffu, (eb >> 1) & 1u);
+                                        if (lane == 0) {
+                                            ex0[t * cat.epitch + m] = ((unsigned long long)a1 << 32) | a0;
+                                            ex0[t * cat.epitch + m + 1] = ((unsigned long long)b1 << 32) | b0;
+                                        }
+                                    }
+                                    if (EXT) {  // values with e > 0 are below 2^-188: no contribution
+                                        if (ea) P.x = 0.f;
+                                        if (eb) P.y = 0.f;
                                     }
                                 } else {
                                     // the sectoral m = l (the FP64 seed, X = 0), or the block's last odd m
@@ -851,14 +886,17 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                     for (int h = 0; h < 2; ++h) {
                                         const int mlh = ml + h, mh = m + h;
                                         float Pq = 0.f, Xq = 0.f;
+                                        unsigned e = 0;
                                         if (mlh < mhi) {  // warp-uniform
                                             const int si = ((mlh >> 1) * KT + q) * 2 + (mlh & 1);
                                             if (l == 0) {
                                                 Pq = P00_SCALED;
                                             } else if (mh == l) {
                                                 Pq = stg1[si];
+                                                if (EXT) e = ebits(stge1[mlh], q);
                                             } else {
                                                 const float p1 = stg1[si], x1 = stg2[si];
+                                                if (EXT) e = ebits(stge1[mlh], q);
                                                 const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
                                                 if (mh >= MR_STD) {
                                                     const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
@@ -872,11 +910,22 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                                     Pq = (mh == 0) ? sum_once(r_hi, r_lo, p1, Xq)
                                                                    : fmaf(r_hi, p1, fmaf(r_lo, p1, Xq));
                                                 }
+                                                if (EXT && e > 0 && fabsf(Pq) > 0x1p40f) {
+                                                    Pq = Pq * 0x1p-64f * 0x1p-64f;
+                                                    Xq = Xq * 0x1p-64f * 0x1p-64f;
+                                                    --e;
+                                                }
                                             }
                                             if (wrows) {
                                                 rowp[h] = Pq;
                                                 xrowp[h] = Xq;
                                             }
+                                            if (EXT && wrows) {
+                                                const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
+                                                const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
+                                                if (lane == 0) ex0[t * cat.epitch + mh] = ((unsigned long long)b1w << 32) | b0w;
+                                            }
+                                            if (EXT && e != 0) Pq = 0.f;  // below 2^-188: no contribution
                                         }
                                         pv[h] = Pq;
                                     }
@@ -1095,9 +1144,11 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
 // slot m = l of the P_{l-1} row set for l = 1 .. lmax-1.  Extended range: in the
 // frame of the running 2-bit exponent (stored value P 2^100 2^(128 e), e raised when
 // the value drops below 2^-40, 0 below 2^-520), with the exponent word written too.
+// mode bit 0: Reinsch-modified rows (sets by the parity of l, records carrying 1 - |cos(theta)|);
+// bit 1: extended range (exponent words, sets of the three-term rows rotating with l % 3)
 __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const double *__restrict__ asect,
                                  int64_t ntiles, int mode) {
-    const bool ext = (mode == 2);
+    const bool rs = (mode & 1) != 0, ext = (mode & 2) != 0;
     const SplitCat c = cats[cat];
     const int64_t t = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
     if (t >= ntiles) return;  // warp-uniform
@@ -1106,14 +1157,14 @@ __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const 
     const SplitPt &pt = c.pts[i];
     // sin(theta): stored (extended range), or from eps = 1 - |cos(theta)| as sqrt(eps (2 - eps))
     const double sv = (double)pt.s_hi + (double)pt.s_lo;
-    const double s = mode == 1 ? sqrt(sv * (2.0 - sv)) : sv;
+    const double s = rs ? sqrt(sv * (2.0 - sv)) : sv;
     const size_t set = (size_t)c.stride * c.lrp;
     float *rt = c.rows + 2 * i;  // this point in the pair-interleaved rows
     double P = (double)P00_SCALED;
     unsigned e = 0;
     for (int l = 1; l < lmax; ++l) {
         P = asect[l] * s * P;
-        const int k = mode == 1 ? (l + 1) & 1 : (l + 2) % 3;  // the set of P_{l-1}
+        const int k = rs ? (l + 1) & 1 : (l + 2) % 3;  // the set of P_{l-1} (and of its exponent words)
         float v;
         if (ext) {
             double f = P;
@@ -1173,7 +1224,7 @@ __global__ void k_split_reduce(const float *__restrict__ partial, int lp1, const
 // that record is padding), and record 16 carries the tile's max |dr| instead: the J
 // operand of a tile whose radii lie close together comes from a Taylor expansion
 // about r_c (k_split_l).  One warp per tile (blockDim a multiple of 32).
-// Plain form (rows of the Reinsch-modified recurrence): the rows are evaluated at
+// Reinsch-modified rows (`plain` set): the rows are evaluated at
 // |cos(theta)|, since P_lm(-x) = (-1)^(l+m) P_lm(x): a point of the southern hemisphere
 // takes phi + pi (the factor (-1)^m of the phase), bit 0 of its phase fraction records
 // the hemisphere and k_split_l applies (-1)^l through its J weight.  The record then
@@ -1524,7 +1575,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             k_split_l<false, true, 2, false>, k_split_l<false, false, 2, false>, k_split_l<false, true, 3, false>,
             k_split_l<false, false, 3, false>, k_split_l<false, true, 2, true>,  k_split_l<false, false, 2, true>,
             k_split_l<false, true, 3, true>,  k_split_l<false, false, 3, true>,  k_split_l<true, true, 2, false>,
-            k_split_l<true, false, 2, false>};
+            k_split_l<true, false, 2, false>, k_split_l<true, true, 2, true>,   k_split_l<true, false, 2, true>};
         for (auto kf : kerns)
             CG_CUDA_TRY(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
         ctx->attr_split = true;
@@ -1616,18 +1667,21 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         int lmax_g = 0;
         for (int c = c0; c < c1; ++c) lmax_g = std::max(lmax_g, cats[c].in.lmax);
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
-        // row sets: plain form P_l, X_l by the parity of l (X = D or P_{l-1}); extended range
-        // P_l, P_{l-1}, P_{l-2} rotating
-        const bool rs = accurate && !ext;  // Reinsch-modified rows (CATANA_SPLIT_ACCURATE)
+        // row sets: Reinsch-modified rows P_l, X_l by the parity of l (X = D or P_{l-1});
+        // three-term rows P_l, P_{l-1}, P_{l-2} rotating
+        const bool rs = accurate;  // Reinsch-modified rows (CATANA_SPLIT_ACCURATE)
         const int nsets = rs ? 4 : 3;
         // three stages (tiles staged two ahead) where shared memory allows: plain rows and a
         // table of at most ~750 intervals; otherwise two
-        const int nst = (!ext && smem_bytes(false, 3, nint) <= SMEM_LIMIT) ? 3 : 2;
-        const uint32_t smem = smem_bytes(ext, nst, nint);
+        const int nst = (!ext && smem_bytes(false, rs, 3, nint) <= SMEM_LIMIT) ? 3 : 2;
+        const uint32_t smem = smem_bytes(ext, rs, nst, nint);
         // kernel per level: extended-range rows above lmax 256; the full-J layout when every
         // item of the level has 128 radial orders in its half
         auto kern_for = [&](bool full) {
-            if (ext) return full ? k_split_l<true, true, 2, false> : k_split_l<true, false, 2, false>;
+            if (ext) {
+                if (rs) return full ? k_split_l<true, true, 2, true> : k_split_l<true, false, 2, true>;
+                return full ? k_split_l<true, true, 2, false> : k_split_l<true, false, 2, false>;
+            }
             if (rs) {
                 if (nst == 3) return full ? k_split_l<false, true, 3, true> : k_split_l<false, false, 3, true>;
                 return full ? k_split_l<false, true, 2, true> : k_split_l<false, false, 2, true>;
@@ -1689,11 +1743,11 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         };
         std::vector<size_t> o_kz(gn), o_nl(gn), o_tm(gn);
         for (int c = c0; c < c1; ++c) {
-            // TMA descriptors: the three Legendre row sets (m pairs interleaved per point:
-            // [lrp / 2][2 stride] FP32, 64 x 16 boxes = 32 m x 32 points)
-            // and, extended range, the three exponent sets ([tile][epitch] words, 128 x 1 boxes)
+            // TMA descriptors 0..3: the Legendre row sets (m pairs interleaved per point:
+            // [lrp / 2][2 stride] FP32, 64 x 16 boxes = 32 m x 32 points); 4..6, extended
+            // range: the exponent sets ([tile][epitch] words, 128 x 1 boxes)
             CatPlan &P = cats[c];
-            CUtensorMap tm[6];
+            CUtensorMap tm[8];
             memset(tm, 0, sizeof(tm));
             char *rows = ws + off_rows[c - c0];
             const uint64_t lrp = (uint64_t)((P.in.lmax + 1) & ~1);
@@ -1708,7 +1762,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 const int ep = (P.in.lmax + 1) & ~1;
                 char *ex = ws + off_exp[c - c0];
                 for (int k = 0; k < 3; ++k)
-                    if (!tmap_2d(&tm[3 + k], CU_TENSOR_MAP_DATA_TYPE_UINT64, ex + (size_t)k * exp_set_words(P) * 8,
+                    if (!tmap_2d(&tm[4 + k], CU_TENSOR_MAP_DATA_TYPE_UINT64, ex + (size_t)k * exp_set_words(P) * 8,
                                  (uint64_t)ep, (uint64_t)P.ntiles, (uint64_t)ep * 8, 128, 1)) {
                         set_error("cuTensorMapEncodeTiled failed for the row exponents");
                         return CATANA_ERR_CUDA;
@@ -1957,7 +2011,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 k_split_sectoral<<<ceil_div(nt, 8), 256, 0, st>>>(reinterpret_cast<const SplitCat *>(pd + o_cats),
                                                                   c - c0, cats[c].in.lmax,
                                                                   reinterpret_cast<const double *>(pd + o_as), nt,
-                                                                  ext ? 2 : (rs ? 1 : 0));
+                                                                  (ext ? 2 : 0) | (rs ? 1 : 0));
                 count_launch();
             }
             CG_CUDA_TRY(cudaGetLastError());

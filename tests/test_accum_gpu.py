@@ -67,16 +67,18 @@ def test_accum_float32_records_vs_oracle(sm103):
     _check(r, f, c, "accum float32 records")
 
 
-def test_accum_float32_large_shape(sm103):
-    """lmax = 512, nmax = 256 (extended rows, two radial halves) through float32 chunks."""
+@pytest.mark.parametrize("form", ["split", "split_accurate"])
+def test_accum_float32_large_shape(sm103, form):
+    """lmax = 512, nmax = 256 (extended rows, two radial halves) through float32 chunks,
+    three-term and Reinsch-modified rows."""
     pts32 = uniform_ball(3000, 1500.0, seed=63).astype(np.float32)
-    with catana.SFBAccumulator(512, 256, 1500.0, precision="split") as acc:
+    with catana.SFBAccumulator(512, 256, 1500.0, precision=form) as acc:
         for p in _chunks(pts32, 2):
             acc.add(p)
         r = acc.finish(store_flmn=True)
     rp = catana.sfb_decomposition(catana.PointContainer(pts32.astype(np.float64)), 512, 256, 1500.0, True, False,
                                   interpolation="off")
-    _check(r, rp.f_lmn, rp.c_ln, "accum float32 lmax 512 nmax 256")
+    _check(r, rp.f_lmn, rp.c_ln, "accum float32 lmax 512 nmax 256 %s" % form)
 
 
 def test_accum_errors(cuda_device):
