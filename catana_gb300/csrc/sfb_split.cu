@@ -72,13 +72,17 @@ namespace catana_gpu {
 namespace {
 
 constexpr int KT = 32;              // points per tile (two K=16 MMA steps)
-constexpr int NTHR = 512;           // 16 operand warps
+constexpr int NOPW = 16;            // operand warps
+constexpr int NTHR = 32 * NOPW;
+constexpr int QPW = (32 + NOPW - 1) / NOPW;   // most quads of complex m per operand warp (128 m = 32 quads)
+constexpr int JPW = (64 + NOPW - 1) / NOPW;   // most J row pairs per operand warp (128 rows)
+static_assert(JPW <= 16, "k_split_l: one lane per J row in the Taylor coefficients");
 constexpr int NFOLDW = 4;           // fold / MMA warps, one per TMEM lane quadrant
 constexpr int NTOT = NTHR + 32 * NFOLDW;
 constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
 constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
 constexpr int FLUSH_FOLDS = 128;    // folds into the TMEM sum before it goes to global memory
-constexpr int NINT_MAX = 1664;      // table intervals resident in shared memory
+constexpr int NINT_MAX = 1664 - (NOPW * JPW - 64);  // table intervals resident in shared memory (lmax 512, nmax 256 at r <= rmax: 1522)
 constexpr double H = 1.0;           // table interval width in z (intervals centred on integers)
 constexpr int TDEG = 6;             // table polynomial degree (7 coefficients in two float4)
 constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 (see header comment)
@@ -117,7 +121,7 @@ __host__ __device__ constexpr uint32_t off_jt(bool ext, bool rs, int nst) {
     return off_rcoef(ext, rs, nst) + (ext && !rs ? 0u : MBLK * 16);
 }
 __host__ __device__ constexpr uint32_t off_tab(bool ext, bool rs, int nst) {
-    return off_jt(ext, rs, nst) + (NTHR / 32) * 32 * 4;
+    return off_jt(ext, rs, nst) + (uint32_t)NOPW * JPW * 8 * 4;
 }
 // dynamic shared memory of a launch (+ 1024 B of alignment slack)
 constexpr uint32_t smem_bytes(bool ext, bool rs, int nst, int nint) {
@@ -207,23 +211,6 @@ __device__ __forceinline__ void store_split8p(uint8_t *hi_base, uint8_t *lo_base
     *reinterpret_cast<uint4 *>(lo_base + off) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
-// Columns 4j .. 4j+3 from two value pairs (8 bytes of each half).
-__device__ __forceinline__ void store_split4p(uint8_t *hi_base, uint8_t *lo_base, uint32_t off, float2 v0, float2 v1) {
-    const float2 v[2] = {v0, v1};
-    uint32_t h[2], o[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        __half2 hh = __float22half2_rn(v[k]);
-        const float2 hf = __half22float2(hh);
-        const float2 lo = __fadd2_rn(v[k], make_float2(-hf.x, -hf.y));
-        __half2 ll = __float22half2_rn(lo);
-        h[k] = *reinterpret_cast<uint32_t *>(&hh);
-        o[k] = *reinterpret_cast<uint32_t *>(&ll);
-    }
-    *reinterpret_cast<uint2 *>(hi_base + off) = make_uint2(h[0], h[1]);
-    *reinterpret_cast<uint2 *>(lo_base + off) = make_uint2(o[0], o[1]);
-}
-
 // 2-bit row exponent of point q from an exponent word (bit q of each half)
 __device__ __forceinline__ unsigned ebits(unsigned long long w, int q) {
     return (unsigned)((w >> q) & 1ull) | ((unsigned)((w >> (32 + q)) & 1ull) << 1);
@@ -250,8 +237,8 @@ __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c
 // shrinks by one when a value grows past 2^40 along l, so seeds down to ~2^-520 stay
 // exact.  Values with e > 0 are below 2^-188 and enter Y as zero.
 // FULLJ: every item of the launch has 128 radial orders in its half (no kmax cut):
-// each warp evaluates 8 J rows; otherwise the items' live row pairs are spread over
-// the warps and the rest of J stays zero.
+// with 16 operand warps each evaluates 8 J rows; otherwise the items' live row pairs
+// are spread over the warps and the rest of J stays zero.
 // one arrival (release, CTA scope) on an mbarrier
 __device__ __forceinline__ void ws_arrive(uint64_t *mbar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc05::smem_u32(mbar)) : "memory");
@@ -405,10 +392,11 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
 
     const int64_t t0 = item.t0, t1 = item.t1;
     const int q = lane, g = warp;
-    // this warp's m: pairs [pb0, pb1) of the block's ceil(mcount / 2) pairs, spread evenly
-    const int npairs = (mcount + 1) >> 1;
-    const int pb0 = (g * npairs) >> 4, pb1 = ((g + 1) * npairs) >> 4;
-    const int mlo = 2 * pb0, mhi = min(2 * pb1, mcount);  // local m range of this warp
+    // this warp's m: quads [qb0, qb1) of the block's ceil(mcount / 4) quads of complex m, spread
+    // evenly (a quad fills one 16-byte column group of each Y half: whole-chunk stores)
+    const int nquads = (mcount + 3) >> 2;
+    const int qb0 = (g * nquads) / NOPW, qb1 = ((g + 1) * nquads) / NOPW;
+    const int mlo = 4 * qb0, mhi = min(4 * qb1, mcount);  // local m range of this warp
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
     const size_t set = (size_t)stride * cat.lrp;
@@ -587,13 +575,31 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
                 sm + OFF_ST + (uint32_t)sidx * STG + 2 * SM_STROW + SM_STPTS);
             const unsigned long long *stge2 = stge1 + MBLK;
-            const SplitPt &pt = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
-                                                                    2 * SM_STROW + q * 48);
+            // this thread's point record in three 16-byte loads (at the records' 48-byte stride
+            // these are free of bank conflicts, the fields one by one are not)
+            const uint4 *prec = reinterpret_cast<const uint4 *>(sm + OFF_ST + (uint32_t)sidx * STG +
+                                                                2 * SM_STROW + q * 48);
+            const uint4 pr0 = prec[0], pr1 = prec[1], pr2 = prec[2];
+            struct {
+                float r_hi, r_lo, w, x_hi, x_lo, s_hi, s_lo, cphi, sphi, dr;
+                unsigned long long u;
+            } pt;
+            pt.r_hi = __uint_as_float(pr0.x);
+            pt.r_lo = __uint_as_float(pr0.y);
+            pt.w = __uint_as_float(pr0.z);
+            pt.x_hi = __uint_as_float(pr0.w);
+            pt.x_lo = __uint_as_float(pr1.x);
+            pt.s_hi = __uint_as_float(pr1.y);
+            pt.s_lo = __uint_as_float(pr1.z);
+            pt.cphi = __uint_as_float(pr1.w);
+            pt.sphi = __uint_as_float(pr2.x);
+            pt.dr = __uint_as_float(pr2.y);
+            pt.u = ((unsigned long long)pr2.w << 32) | pr2.z;
             const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
             // Reinsch-modified rows: at |cos(theta)|, the factor (-1)^l of a southern point in its weight
             const float wq = (RS && (l & 1) && (pt.u & 1ull)) ? -pt.w : pt.w;
             // ---- J tile: n = 8 g .. 8 g + 7 ----
-            if constexpr (FULLJ) {
+            if constexpr (FULLJ && NOPW == 16) {
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(wq, wq);
                 const int n0 = 8 * g;
@@ -604,7 +610,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                     // J(n, q) = w_q sum_j c'_j dr_q^j about the tile's record-16 radius r_c:
                     // c'_j = 2^s_n k_n^j p^(j)(u0_n) / j!, p the interval polynomial, u0_n the
                     // offset of z_n = k_n r_c in its interval (float-float product)
-                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * g;
                     __syncwarp();
                     if (lane < 8) {
                         const int n = n0 + lane;
@@ -686,15 +692,15 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             }
             else {
                 // fewer radial orders (a kmax cut, nmax < 128): their ceil(nmax / 2) row pairs
-                // spread evenly over the 16 warps (the rows past the count stay zero)
+                // spread evenly over the operand warps (the rows past the count stay zero)
                 const int npr = (nmax + 1) >> 1;
-                const int jp0 = (g * npr) >> 4, jp1 = ((g + 1) * npr) >> 4;
+                const int jp0 = (g * npr) / NOPW, jp1 = ((g + 1) * npr) / NOPW;
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(wq, wq);
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
-                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + 32 * g;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * g;
                     __syncwarp();
                     if (lane < 2 * (jp1 - jp0)) {  // rows past the count have k = 0, J scale 0: zero coefficients
                         const int n = 2 * jp0 + lane;
@@ -779,7 +785,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                     *reinterpret_cast<__half2 *>(jlo + off) = ll;
                 }
             }
-            // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1) ----
+            // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1), stored by quads ----
             if (mlo < mhi) {
                 // x = cos(theta) (Reinsch-modified rows: |cos(theta)|) and eps = 1 - |cos(theta)|
                 const float xh = pt.x_hi, xl = pt.x_lo, eh = pt.s_hi, el = pt.s_lo, c1 = pt.cphi, s1 = pt.sphi;
@@ -798,11 +804,12 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                 const float2 c22 = make_float2(c2, c2), s22 = make_float2(s2, s2), ns22 = make_float2(-s2, -s2);
                 const float2 xh2 = make_float2(xh, xh), xl2 = make_float2(xl, xl);
                 const float2 eh2 = make_float2(eh, eh), el2 = make_float2(el, el);
+                float2 yq0 = make_float2(0.f, 0.f), yq1 = yq0;  // Y (Re, Im) of the quad's first pair
     #pragma unroll
-                for (int pp = 0; pp < 4; ++pp) {
+                for (int pp = 0; pp < 2 * QPW; ++pp) {
                     const int ml = mlo + 2 * pp;  // even local m
+                    float2 yr = make_float2(0.f, 0.f), yi = yr;
                     if (ml < mhi) {
-                        float2 yr, yi;
                         {
                             const int m = mb0 + ml;
                             float2 P;
@@ -1049,7 +1056,15 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                             nsm = __ffma2_rn(nsm, c22, __fmul2_rn(cm, ns22));
                             cm = cmn;
                         }
-                        store_split4p(yhi, ylo, tc05::mn_sw128_off(2 * ml, q, 4), yr, yi);
+                    }
+                    if (pp & 1) {
+                        // the quad of pairs pp - 1, pp: one 16-byte chunk per half (a second pair past
+                        // the warp's range enters as zeros, in columns the flush never reads)
+                        if (ml - 2 < mhi)
+                            store_split8p(yhi, ylo, tc05::mn_sw128_off(2 * (ml - 2), q, 4), yq0, yq1, yr, yi);
+                    } else {
+                        yq0 = yr;
+                        yq1 = yi;
                     }
                     rowp += 2 * (size_t)stride;
                 }
