@@ -360,6 +360,7 @@ def batched_workload(torch, _lib, catana, sp, ncat=64, seed=4, kmax=0.2, nmax=12
     ms = e0.elapsed_time(e1) / 3
     res = {"value": pm / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "catalogs": ncat,
            "points": int(ns.sum()), "point_modes": pm, "waves_autotuned": _lib.lib.catana_gpu_batch_waves(),
+           "mblock_autotuned": int(_lib.lib.catana_gpu_batch_mblk()),
            "graph": True}
     # subsample (0.5%, at least 1000 points a catalog): split vs FP64 plain with the
     # reference's j_l rule (interpolated for N > 1000) for the throughput ratio, and

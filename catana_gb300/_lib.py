@@ -32,6 +32,7 @@ FORM_PLAIN, FORM_SPLIT = 0, 4
 SPLIT_ACCURATE = 32
 HEALPIX_CONJ_FIX = 8
 BATCH_NO_GRAPH = 16
+BATCH_MBLK64 = 64
 
 
 class Catalog(ctypes.Structure):
@@ -61,6 +62,7 @@ SIGNATURES = {
     "catana_gpu_sfb_raw_batched": (ctypes.c_int, [_P, _I32, _U32, _D, _P]),
     "catana_gpu_sfb_raw_batched_dev": (ctypes.c_int, [_P, _I32, _U32, _D, _P, _P]),
     "catana_gpu_batch_waves": (ctypes.c_double, []),
+    "catana_gpu_batch_mblk": (ctypes.c_int32, []),
     "catana_gpu_accum_create": (ctypes.c_int, [_U16, _U16, _D, _U32, _P]),
     "catana_gpu_accum_add_f32": (ctypes.c_int, [_P, _P, _P, _I64]),
     "catana_gpu_accum_add": (ctypes.c_int, [_P, _P, _P, _I64]),

@@ -390,7 +390,8 @@ catana_status_t batched_device(DeviceContext *ctx, const catana_catalog_t *cats,
                 v.push_back(in);
             }
         }
-        s = split_run(ctx, v, !(flags & CATANA_BATCH_NO_GRAPH), waves, err_d, st);
+        s = split_run(ctx, v, !(flags & CATANA_BATCH_NO_GRAPH), waves, (flags & CATANA_BATCH_MBLK64) ? 64 : 128,
+                      err_d, st);
         if (s != CATANA_OK) return s;
     } else {
         for (int c = 0; c < ncat; ++c) {
@@ -706,6 +707,12 @@ double catana_gpu_batch_waves(void) {
     int cs;
     DeviceContext *ctx = get_context(&cs);
     return ctx ? ctx->split_last_waves : 0.0;
+}
+
+int32_t catana_gpu_batch_mblk(void) {
+    int cs;
+    DeviceContext *ctx = get_context(&cs);
+    return ctx ? ctx->split_last_mblk : 0;
 }
 
 catana_status_t catana_gpu_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

@@ -76,8 +76,9 @@ struct DeviceContext {
     DevBuf split_tab;  // split-form tables
     DevBuf split_plan; // split-form plan (catalog descriptors, items, reductions)
     SplitCache split_cache;
-    std::map<std::string, double> split_tuned;  // autotuned waves per catalog set
+    std::map<std::string, std::pair<double, int>> split_tuned;  // autotuned (waves, m-block cap) per catalog set
     double split_last_waves = 0.0;
+    int split_last_mblk = 0;
     cudaStream_t capture_stream = nullptr;      // stream the split level loop is captured on
     cudaEvent_t split_ws_event = nullptr;       // end of the last split run (orders workspace reuse across streams)
     DevBuf hp_ws;      // HEALPix workspace
@@ -145,9 +146,10 @@ struct SplitCatInput {
 };
 // Split form over several catalogs: level-synchronous launches over all of them,
 // optionally captured as one CUDA graph.  `waves` = CTAs per SM each level's work
-// items are cut for; <= 0 autotunes it (timed sample levels, cached per catalog set).
+// items are cut for, `mblk` the most complex m per work item (128 or 64); waves <= 0
+// autotunes both (timed sample levels, cached per catalog set).
 catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats, bool use_graph, double waves,
-                          int *err_dev, cudaStream_t st);
+                          int mblk, int *err_dev, cudaStream_t st);
 
 // Convert, filter and compact n device records (ingest.cu); *n_out kept, in order.
 catana_status_t ingest_dev(DeviceContext *ctx, const void *rec_dev, int64_t n, const catana_ingest_t &spec,

@@ -1582,7 +1582,8 @@ std::string tune_key(const std::vector<CatPlan> &cats, int c0, int c1) {
 std::atomic<uint64_t> g_split_stall_ns{0};
 
 catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_in, bool use_graph,
-                          double waves, int *err_dev, cudaStream_t st) {
+                          double waves, int mblk_cap, int *err_dev, cudaStream_t st) {
+    if (mblk_cap != 64) mblk_cap = MBLK;
     // every catalog of a call carries the same flags
     const bool accurate = !cats_in.empty() && cats_in.front().accurate;
     std::vector<CatPlan> cats;
@@ -1854,9 +1855,10 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.nmax_l = nullptr;
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
-        // Work items of every level for a schedule of `waves` CTAs per SM: at level l
-        // the group's tiles x m-blocks are cut into slabs of T tiles, T chosen so the
-        // items fill about waves x SMs CTAs.  Items of one catalog are block-major.
+        // Work items of every level for a schedule of `waves` CTAs per SM and m-blocks of at
+        // most `mcap` complex m (the MMA's N = 2 mcount): at level l the group's tiles x
+        // m-blocks are cut into slabs of T tiles, T chosen so the items fill about waves x SMs
+        // CTAs.  Items of one catalog are block-major.
         struct Sched {
             std::vector<SplitItem> items;
             std::vector<SplitRed> reds;
@@ -1864,7 +1866,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             std::vector<char> fullj;  // per level: every item has 128 radial orders in its half
             std::vector<double> flops;
         };
-        auto schedule = [&](double waves, Sched &S) {
+        auto schedule = [&](double waves, int mcap, Sched &S) {
             S.items.clear();
             S.reds.clear();
             S.item0.assign(lmax_g + 1, 0);
@@ -1875,7 +1877,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             for (int l = 0; l < lmax_g; ++l) {
                 S.item0[l] = (int)S.items.size();
                 S.red0[l] = (int)S.reds.size();
-                const int nblocks = (l + 1 + MBLK - 1) / MBLK;
+                const int nblocks = (l + 1 + mcap - 1) / mcap;
                 const int mblk = (((l + 1 + nblocks - 1) / nblocks) + 3) & ~3;  // balanced, multiple of 4
                 // the active catalogs, largest first: the CTAs of a launch start
                 // roughly in index order, so the long items start first
@@ -1985,25 +1987,31 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         };
 
         double waves_use = waves;
+        int mblk_use = mblk_cap;
         if (waves_use <= 0.0) {
             // autotune: time the contraction at three sample levels for each schedule
             // (the rows those launches write are rewritten by the real level loop)
             const std::string key = tune_key(cats, c0, c1);
             auto hit = ctx->split_tuned.find(key);
             if (hit != ctx->split_tuned.end()) {
-                waves_use = hit->second;
+                waves_use = hit->second.first;
+                mblk_use = hit->second.second;
             } else {
+                // the schedule (CTAs per SM) and the tile shape (m-block width: the MMA's N)
                 const double cand[] = {1.0, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0};
+                const int mcand[] = {MBLK, 64};
                 const int ls[3] = {std::max(1, lmax_g / 4), std::max(1, lmax_g / 2), std::max(1, (3 * lmax_g) / 4)};
                 cudaEvent_t e0, e1;
                 CG_CUDA_TRY(cudaEventCreate(&e0));
                 CG_CUDA_TRY(cudaEventCreate(&e1));
                 double best = 1e300;
                 waves_use = 1.0;
+                mblk_use = MBLK;
                 Sched S;
                 for (int rep = 0; rep < 2; ++rep)
+                    for (int mc : mcand)
                     for (double w : cand) {
-                        schedule(w, S);
+                        schedule(w, mc, S);
                         s = upload(S);
                         if (s != CATANA_OK) return s;
                         CG_CUDA_TRY(cudaEventRecord(e0, st));
@@ -2022,16 +2030,18 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                         if (rep == 1 && ms < best) {
                             best = ms;
                             waves_use = w;
+                            mblk_use = mc;
                         }
                     }
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
-                ctx->split_tuned[key] = waves_use;
+                ctx->split_tuned[key] = std::make_pair(waves_use, mblk_use);
             }
         }
         ctx->split_last_waves = waves_use;
+        ctx->split_last_mblk = mblk_use;
         Sched S;
-        schedule(waves_use, S);
+        schedule(waves_use, mblk_use, S);
         s = upload(S);
         if (s != CATANA_OK) return s;
         float *partial = ctx->partial.as<float>();
@@ -2119,7 +2129,7 @@ catana_status_t split_raw_accumulate(DeviceContext *ctx, const double *points_de
         in.accurate = accurate;
         v.push_back(in);
     }
-    return split_run(ctx, v, false, 1.0, err_dev, st);
+    return split_run(ctx, v, false, 1.0, MBLK, err_dev, st);
 }
 
 }  // namespace catana_gpu

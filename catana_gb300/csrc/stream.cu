@@ -146,7 +146,7 @@ catana_status_t accum_add(Accum *A, const T *points, const T *weights, int64_t n
             in.accurate = (A->flags & CATANA_SPLIT_ACCURATE) != 0;
             v.push_back(in);
         }
-        s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);
+        s = split_run(ctx, v, false, 1.0, 128, err_d, A->comp_st);
     } else {
         const double *p64 = reinterpret_cast<const double *>(pd), *w64 = reinterpret_cast<const double *>(wd);
         if (sizeof(T) == 4) {  // the FP64 path reads float64 records
@@ -231,7 +231,7 @@ catana_status_t accum_add_records(Accum *A, const void *records, int64_t n, cons
                 in.accurate = (A->flags & CATANA_SPLIT_ACCURATE) != 0;
                 v.push_back(in);
             }
-            s = split_run(ctx, v, false, 1.0, err_d, A->comp_st);
+            s = split_run(ctx, v, false, 1.0, 128, err_d, A->comp_st);
         } else {
             const uint32_t jl = A->flags & CATANA_JL_MASK;
             const JlMode mode =

@@ -187,15 +187,18 @@ def sfb_decomposition_healpix(pixelized_point_container, lmax, nmax, rmax, store
 
 
 def sfb_decomposition_batched(point_containers, lmax, nmax, rmax, kmax=None, weights=None, store_flmn=False,
-                              verbose=True, precision="split", interpolation="auto", waves=0.0, graph=True):
+                              verbose=True, precision="split", interpolation="auto", waves=0.0, graph=True,
+                              mblock=128):
     """Decompose many catalogs in one call (no counterpart in the reference).
 
     point_containers: sequence of PointContainer (or (N, 3) arrays of r, theta, phi).
     lmax, nmax, rmax, kmax, weights: one value for all catalogs or one per catalog;
     kmax > 0 keeps only the modes with k_ln <= kmax (the others have f = C = 0).
     precision='split' runs all catalogs level by level in grouped tcgen05 launches,
-    captured as one CUDA graph (graph=False launches the levels directly); waves <= 0
-    autotunes the work-item size.  precision='plain' runs the FP64 path per catalog.
+    captured as one CUDA graph (graph=False launches the levels directly); waves sets
+    the work items per SM and mblock (128 or 64) the most complex m per work item (the
+    MMA tile's N); waves <= 0 autotunes both.  precision='plain' runs the FP64 path per
+    catalog.
     Returns a list of KClkk.
     """
     cats = list(point_containers)
@@ -213,7 +216,10 @@ def sfb_decomposition_batched(point_containers, lmax, nmax, rmax, kmax=None, wei
     rmaxs = per(rmax, "rmax", float)
     kmaxs = per(0.0 if kmax is None else kmax, "kmax", lambda x: 0.0 if x is None else float(x))
     ws = [None] * nc if weights is None else per(weights, "weights", lambda x: x)
-    flags = _flags(interpolation, precision) | (0 if graph else _lib.BATCH_NO_GRAPH)
+    if mblock not in (128, 64):
+        raise ValueError("mblock must be 128 or 64")
+    flags = _flags(interpolation, precision) | (0 if graph else _lib.BATCH_NO_GRAPH) | \
+        (_lib.BATCH_MBLK64 if mblock == 64 else 0)
     recs = (_lib.Catalog * max(nc, 1))()
     keep, out = [], []
     for i, pc in enumerate(cats):

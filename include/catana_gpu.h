@@ -156,14 +156,18 @@ typedef struct {
 /* Batched flags (combine with CATANA_FORM_* and, for the plain form, CATANA_JL_*). */
 #define CATANA_BATCH_NO_GRAPH 16u  /* split form: launch the level loop directly
                                       instead of capturing it as one CUDA graph */
+#define CATANA_BATCH_MBLK64 64u    /* split form, fixed schedule (waves > 0): work items of
+                                      at most 64 complex m instead of 128 */
 
 /* Split form: the catalogs advance level by level together -- at each l one
  * grouped tcgen05 launch covers every catalog's (m-block, tile-slab) work items and
  * one grouped reduction folds them into each catalog's f -- and the whole level
  * loop is captured and launched as one CUDA graph.  `waves` sets how many CTAs per
- * SM each level's items are cut for; waves <= 0 autotunes it (times the
- * contraction at three sample levels for several schedules, once per distinct
- * catalog set; catana_gpu_batch_waves() reports the choice).  Plain form: the
+ * SM each level's items are cut for, and the work items hold at most 128 complex m
+ * (64 with CATANA_BATCH_MBLK64: the MMA tile's N, 2 m per column pair); waves <= 0
+ * autotunes both -- the schedule and the tile shape -- by timing the contraction at
+ * three sample levels for each candidate, once per distinct catalog set
+ * (catana_gpu_batch_waves() and catana_gpu_batch_mblk() report the choice).  Plain form: the
  * catalogs run one after another through the FP64 path (waves ignored).
  * Host pointers in the catalog records; blocks until the results are in place. */
 catana_status_t catana_gpu_sfb_raw_batched(const catana_catalog_t *cats, int32_t ncat, uint32_t flags, double waves,
@@ -177,6 +181,8 @@ catana_status_t catana_gpu_sfb_raw_batched_dev(const catana_catalog_t *cats, int
 
 /* Waves per SM the last split-form run used (the autotuned value when it tuned). */
 double catana_gpu_batch_waves(void);
+/* Most complex m per work item of the last split-form run (128 or 64). */
+int32_t catana_gpu_batch_mblk(void);
 
 /* ---- chunked accumulation of one large catalog (no counterpart in the reference) --
  * For catalogs streamed from disk or host memory in chunks (the reference's

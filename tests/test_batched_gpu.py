@@ -45,11 +45,11 @@ def batch():
     return pts, ws, ref
 
 
-def _run(pts, ws, precision="split", waves=2.0, graph=True):
+def _run(pts, ws, precision="split", waves=2.0, graph=True, mblock=128):
     return catana.sfb_decomposition_batched(
         [catana.PointContainer(p) for p in pts], [c[1] for c in CATS], [c[2] for c in CATS],
         [c[3] for c in CATS], kmax=[c[4] for c in CATS], weights=ws, store_flmn=True, verbose=False,
-        precision=precision, waves=waves, graph=graph)
+        precision=precision, waves=waves, graph=graph, mblock=mblock)
 
 
 def _keep(k, kmax):
@@ -101,11 +101,25 @@ def test_batched_graph_equals_direct_launches(sm103, batch):
             assert np.array_equal(fx, fy)
 
 
+def test_batched_mblock64(sm103, batch):
+    """Work items of at most 64 complex m (the MMA tile's N = 128): levels l >= 64 split
+    into two or three m-blocks; every catalog keeps the bar against the oracle."""
+    pts, ws, ref = batch
+    res = _run(pts, ws, waves=2.0, mblock=64)
+    assert _lib.lib.catana_gpu_batch_mblk() == 64
+    for i, (r, (k, c, f)) in enumerate(zip(res, ref)):
+        _check_cut(r, k, c, f, CATS[i][4], "mblock 64 catalog %d" % i)
+    with pytest.raises(ValueError):
+        _run(pts, ws, mblock=32)
+
+
 def test_batched_autotune(sm103, batch):
-    """waves <= 0 picks a schedule from the candidate set; the result keeps the bar."""
+    """waves <= 0 picks a schedule and a tile shape from the candidate sets; the result
+    keeps the bar."""
     pts, ws, ref = batch
     res = _run(pts, ws, waves=0.0)
     assert _lib.lib.catana_gpu_batch_waves() in (1.0, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0)
+    assert _lib.lib.catana_gpu_batch_mblk() in (128, 64)
     for i, (r, (k, c, f)) in enumerate(zip(res, ref)):
         _check_cut(r, k, c, f, CATS[i][4], "autotuned catalog %d" % i)
     again = _run(pts, ws, waves=0.0)  # cached choice: same schedule, same bits
