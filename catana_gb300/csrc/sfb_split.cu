@@ -74,19 +74,15 @@ namespace {
 constexpr int KT = 32;              // points per tile (two K=16 MMA steps)
 constexpr int NOPW = 16;            // operand warps
 constexpr int NTHR = 32 * NOPW;
-constexpr int NYW = 0;              // operand warps writing only Y (0: every operand warp writes J and Y)
-constexpr int YW = NYW ? NYW : NOPW;          // warps writing Y
-constexpr int NJW = NYW ? NOPW - NYW : NOPW;  // warps writing J
-constexpr int RJW = 128 / NJW;                // J rows per J warp when every radial order is live
-constexpr int QPW = (32 + YW - 1) / YW;       // most quads of complex m per Y warp (128 m = 32 quads)
-constexpr int JPW = (64 + NJW - 1) / NJW;     // most J row pairs per J warp (128 rows)
+constexpr int QPW = (32 + NOPW - 1) / NOPW;   // most quads of complex m per operand warp (128 m = 32 quads)
+constexpr int JPW = (64 + NOPW - 1) / NOPW;   // most J row pairs per operand warp (128 rows)
 static_assert(JPW <= 16, "k_split_l: one lane per J row in the Taylor coefficients");
 constexpr int NFOLDW = 4;           // fold / MMA warps, one per TMEM lane quadrant
 constexpr int NTOT = NTHR + 32 * NFOLDW;
 constexpr int MBLK = 128;           // complex m per CTA block (256 accumulator columns)
 constexpr int FOLD_TILES = 1;       // tiles accumulated by the tensor core before a fold into D_acc (2 doubles the C_l error)
 constexpr int FLUSH_FOLDS = 128;    // folds into the TMEM sum before it goes to global memory
-constexpr int NINT_MAX = 1664 - (NJW * JPW - 64);  // table intervals resident in shared memory (lmax 512, nmax 256 at r <= rmax: 1522)
+constexpr int NINT_MAX = 1664 - (NOPW * JPW - 64);  // table intervals resident in shared memory (lmax 512, nmax 256 at r <= rmax: 1522)
 constexpr double H = 1.0;           // table interval width in z (intervals centred on integers)
 constexpr int TDEG = 6;             // table polynomial degree (7 coefficients in two float4)
 constexpr int SPLIT_LMAX = 256;     // rows scaled by 2^100 alone cover l < 256 (see header comment)
@@ -125,7 +121,7 @@ __host__ __device__ constexpr uint32_t off_jt(bool ext, bool rs, int nst) {
     return off_rcoef(ext, rs, nst) + (ext && !rs ? 0u : MBLK * 16);
 }
 __host__ __device__ constexpr uint32_t off_tab(bool ext, bool rs, int nst) {
-    return off_jt(ext, rs, nst) + (uint32_t)NJW * JPW * 8 * 4;
+    return off_jt(ext, rs, nst) + (uint32_t)NOPW * JPW * 8 * 4;
 }
 // dynamic shared memory of a launch (+ 1024 B of alignment slack)
 constexpr uint32_t smem_bytes(bool ext, bool rs, int nst, int nint) {
@@ -398,12 +394,8 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     const int q = lane, g = warp;
     // this warp's m: quads [qb0, qb1) of the block's ceil(mcount / 4) quads of complex m, spread
     // evenly (a quad fills one 16-byte column group of each Y half: whole-chunk stores)
-    // (with NYW > 0 the operand warps split by role: warps 0 .. NYW-1 write Y, the rest J)
-    const bool do_j = NYW == 0 || g >= NYW;
-    const int gj = NYW == 0 ? g : g - NYW;  // index among the J warps
     const int nquads = (mcount + 3) >> 2;
-    const int qb0 = (NYW == 0 || g < NYW) ? (g * nquads) / YW : 0;
-    const int qb1 = (NYW == 0 || g < NYW) ? ((g + 1) * nquads) / YW : 0;
+    const int qb0 = (g * nquads) / NOPW, qb1 = ((g + 1) * nquads) / NOPW;
     const int mlo = 4 * qb0, mhi = min(4 * qb1, mcount);  // local m range of this warp
     const uint32_t idesc = tc05::idesc_f16_mn(128, ncols_pad);
     const int stride = cat.stride;
@@ -606,24 +598,22 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             const int64_t i = t * KT + q;  // records past n are zero (w = 0, so their J is 0)
             // Reinsch-modified rows: at |cos(theta)|, the factor (-1)^l of a southern point in its weight
             const float wq = (RS && (l & 1) && (pt.u & 1ull)) ? -pt.w : pt.w;
-            // ---- J tile: this warp's rows (J warps) ----
-            if (do_j) {
-            if constexpr (FULLJ && RJW % 8 == 0) {
-                // every radial order live: RJW consecutive rows n = RJW gj .., in groups of 8
+            // ---- J tile: n = 8 g .. 8 g + 7 ----
+            if constexpr (FULLJ && NOPW == 16) {
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(wq, wq);
-                const int nj0 = RJW * gj;
+                const int n0 = 8 * g;
+                float2 v[4];
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
-                const bool taylor = kmax_j * pc.dr <= JT_TAU;  // the same for every thread of the CTA
-                float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * gj;
-                if (taylor) {
+                if (kmax_j * pc.dr <= JT_TAU) {  // the same for every thread of the CTA
                     // J(n, q) = w_q sum_j c'_j dr_q^j about the tile's record-16 radius r_c:
                     // c'_j = 2^s_n k_n^j p^(j)(u0_n) / j!, p the interval polynomial, u0_n the
-                    // offset of z_n = k_n r_c in its interval (float-float product); one row per lane
+                    // offset of z_n = k_n r_c in its interval (float-float product)
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * g;
                     __syncwarp();
-                    if (lane < RJW) {
-                        const int n = nj0 + lane;
+                    if (lane < 8) {
+                        const int n = n0 + lane;
                         const float4 kk = s_kzp[n >> 1];
                         const float kx = (n & 1) ? kk.y : kk.x, ky = (n & 1) ? kk.w : kk.z;
                         const float p = __fmul_rn(pc.r_hi, kx);
@@ -654,70 +644,63 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                         o[6] = b3 * k3;
                     }
                     __syncwarp();
-                }
-                const float dq = (q == 16) ? 0.f : pt.dr;
-                const float2 d2 = make_float2(dq, dq);
+                    const float dq = (q == 16) ? 0.f : pt.dr;
+                    const float2 d2 = make_float2(dq, dq);
     #pragma unroll
-                for (int s8 = 0; s8 < RJW / 8; ++s8) {
-                    const int n0 = nj0 + 8 * s8;
-                    float2 v[4];
-                    if (taylor) {
-    #pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            const float4 ca = *reinterpret_cast<const float4 *>(cs + 8 * (4 * s8 + k));
-                            const float4 cb = *reinterpret_cast<const float4 *>(cs + 8 * (4 * s8 + k) + 4);
-                            float2 jv = __ffma2_rn(make_float2(cb.z, cb.w), d2, make_float2(cb.x, cb.y));
-                            jv = __ffma2_rn(jv, d2, make_float2(ca.z, ca.w));
-                            jv = __ffma2_rn(jv, d2, make_float2(ca.x, ca.y));
-                            v[k] = __fmul2_rn(jv, w2);
-                        }
-                    } else {
-    #pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            const int n = n0 + 2 * k;
-                            const float4 kk = s_kzp[n >> 1];
-                            const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
-                            // z = r k as float-float: p + e
-                            const float2 p = __fmul2_rn(rh2, kx);
-                            float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
-                            e = __ffma2_rn(rh2, ky, e);
-                            e = __ffma2_rn(rl2, kx, e);
-                            const float2 fl = make_float2(rintf(p.x), rintf(p.y));
-                            const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);  // in [-1/2, 1/2]
-                            // radii are checked on the host against the table's extent; clamp regardless
-                            const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
-                            const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
-                            const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
-                            const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
-                            float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
-                            ja = fmaf(ja, uu.x, a1.x);
-                            jb = fmaf(jb, uu.y, b1.x);
-                            ja = fmaf(ja, uu.x, a0.w);
-                            jb = fmaf(jb, uu.y, b0.w);
-                            ja = fmaf(ja, uu.x, a0.z);
-                            jb = fmaf(jb, uu.y, b0.z);
-                            ja = fmaf(ja, uu.x, a0.y);
-                            jb = fmaf(jb, uu.y, b0.y);
-                            ja = fmaf(ja, uu.x, a0.x);
-                            jb = fmaf(jb, uu.y, b0.x);
-                            const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
-                            v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
-                        }
+                    for (int k = 0; k < 4; ++k) {
+                        const float4 ca = *reinterpret_cast<const float4 *>(cs + 8 * k);
+                        const float4 cb = *reinterpret_cast<const float4 *>(cs + 8 * k + 4);
+                        float2 jv = __ffma2_rn(make_float2(cb.z, cb.w), d2, make_float2(cb.x, cb.y));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.z, ca.w));
+                        jv = __ffma2_rn(jv, d2, make_float2(ca.x, ca.y));
+                        v[k] = __fmul2_rn(jv, w2);
                     }
-                    store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
+                } else {
+    #pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int n = n0 + 2 * k;
+                    const float4 kk = s_kzp[n >> 1];
+                    const float2 kx = make_float2(kk.x, kk.y), ky = make_float2(kk.z, kk.w);
+                    // z = r k as float-float: p + e
+                    const float2 p = __fmul2_rn(rh2, kx);
+                    float2 e = __ffma2_rn(rh2, kx, make_float2(-p.x, -p.y));
+                    e = __ffma2_rn(rh2, ky, e);
+                    e = __ffma2_rn(rl2, kx, e);
+                    const float2 fl = make_float2(rintf(p.x), rintf(p.y));
+                    const float2 uu = __fadd2_rn(__fadd2_rn(p, make_float2(-fl.x, -fl.y)), e);  // in [-1/2, 1/2]
+                    // radii are checked on the host against the table's extent; clamp regardless
+                    const unsigned ia = min((unsigned)(int)fl.x, (unsigned)(a.nint - 1));
+                    const unsigned ib = min((unsigned)(int)fl.y, (unsigned)(a.nint - 1));
+                    const float4 a0 = s_tab[2 * ia], a1 = s_tab[2 * ia + 1];
+                    const float4 b0 = s_tab[2 * ib], b1 = s_tab[2 * ib + 1];
+                    float ja = fmaf(a1.z, uu.x, a1.y), jb = fmaf(b1.z, uu.y, b1.y);
+                    ja = fmaf(ja, uu.x, a1.x);
+                    jb = fmaf(jb, uu.y, b1.x);
+                    ja = fmaf(ja, uu.x, a0.w);
+                    jb = fmaf(jb, uu.y, b0.w);
+                    ja = fmaf(ja, uu.x, a0.z);
+                    jb = fmaf(jb, uu.y, b0.z);
+                    ja = fmaf(ja, uu.x, a0.y);
+                    jb = fmaf(jb, uu.y, b0.y);
+                    ja = fmaf(ja, uu.x, a0.x);
+                    jb = fmaf(jb, uu.y, b0.x);
+                    const float2 js = *reinterpret_cast<const float2 *>(s_js + n);
+                    v[k] = __fmul2_rn(make_float2(ja, jb), __fmul2_rn(w2, js));
                 }
+                }
+                store_split8p(jhi, jlo, tc05::mn_sw128_off(n0, q, 2), v[0], v[1], v[2], v[3]);
             }
             else {
                 // fewer radial orders (a kmax cut, nmax < 128): their ceil(nmax / 2) row pairs
-                // spread evenly over the J warps (the rows past the count stay zero)
+                // spread evenly over the operand warps (the rows past the count stay zero)
                 const int npr = (nmax + 1) >> 1;
-                const int jp0 = (gj * npr) / NJW, jp1 = ((gj + 1) * npr) / NJW;
+                const int jp0 = (g * npr) / NOPW, jp1 = ((g + 1) * npr) / NOPW;
                 const float2 rh2 = make_float2(pt.r_hi, pt.r_hi), rl2 = make_float2(pt.r_lo, pt.r_lo);
                 const float2 w2 = make_float2(wq, wq);
                 const SplitPt &pc = *reinterpret_cast<const SplitPt *>(sm + OFF_ST + (uint32_t)sidx * STG +
                                                                        2 * SM_STROW + 16 * 48);
                 if (kmax_j * pc.dr <= JT_TAU) {  // Taylor form about the tile's record-16 radius (as above)
-                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * gj;
+                    float *cs = reinterpret_cast<float *>(sm + off_jt(EXT, RS, NST)) + JPW * 8 * g;
                     __syncwarp();
                     if (lane < 2 * (jp1 - jp0)) {  // rows past the count have k = 0, J scale 0: zero coefficients
                         const int n = 2 * jp0 + lane;
@@ -801,7 +784,6 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                     *reinterpret_cast<__half2 *>(jhi + off) = hh;
                     *reinterpret_cast<__half2 *>(jlo + off) = ll;
                 }
-            }
             }
             // ---- Y tile: local m = mlo .. mhi-1 of this block, in pairs (m, m+1), stored by quads ----
             if (mlo < mhi) {
@@ -1855,10 +1837,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.nmax_l = nullptr;
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
-        // Work items of every level for a schedule of `waves` CTAs per SM and m-blocks of at
-        // most `mcap` complex m (the MMA's N = 2 mcount): at level l the group's tiles x
-        // m-blocks are cut into slabs of T tiles, T chosen so the items fill about waves x SMs
-        // CTAs.  Items of one catalog are block-major.
+        // Work items of every level for a schedule of `waves` CTAs per SM: at level l
+        // the group's tiles x m-blocks are cut into slabs of T tiles, T chosen so the
+        // items fill about waves x SMs CTAs.  Items of one catalog are block-major.
         struct Sched {
             std::vector<SplitItem> items;
             std::vector<SplitRed> reds;
@@ -1997,21 +1978,17 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 waves_use = hit->second.first;
                 mblk_use = hit->second.second;
             } else {
-                // the schedule (CTAs per SM) and the tile shape (m-block width: the MMA's N)
                 const double cand[] = {1.0, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0};
-                const int mcand[] = {MBLK, 64};
                 const int ls[3] = {std::max(1, lmax_g / 4), std::max(1, lmax_g / 2), std::max(1, (3 * lmax_g) / 4)};
                 cudaEvent_t e0, e1;
                 CG_CUDA_TRY(cudaEventCreate(&e0));
                 CG_CUDA_TRY(cudaEventCreate(&e1));
                 double best = 1e300;
                 waves_use = 1.0;
-                mblk_use = MBLK;
                 Sched S;
                 for (int rep = 0; rep < 2; ++rep)
-                    for (int mc : mcand)
                     for (double w : cand) {
-                        schedule(w, mc, S);
+                        schedule(w, MBLK, S);
                         s = upload(S);
                         if (s != CATANA_OK) return s;
                         CG_CUDA_TRY(cudaEventRecord(e0, st));
@@ -2030,7 +2007,6 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                         if (rep == 1 && ms < best) {
                             best = ms;
                             waves_use = w;
-                            mblk_use = mc;
                         }
                     }
                 cudaEventDestroy(e0);
