@@ -1837,9 +1837,10 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             sc.nmax_l = nullptr;
             memcpy(host.data() + o_cats + (size_t)(c - c0) * sizeof(SplitCat), &sc, sizeof(SplitCat));
         }
-        // Work items of every level for a schedule of `waves` CTAs per SM: at level l
-        // the group's tiles x m-blocks are cut into slabs of T tiles, T chosen so the
-        // items fill about waves x SMs CTAs.  Items of one catalog are block-major.
+        // Work items of every level for a schedule of `waves` CTAs per SM and m-blocks of at
+        // most `mcap` complex m (the MMA's N = 2 mcount): at level l the group's tiles x
+        // m-blocks are cut into slabs of T tiles, T chosen so the items fill about waves x SMs
+        // CTAs.  Items of one catalog are block-major.
         struct Sched {
             std::vector<SplitItem> items;
             std::vector<SplitRed> reds;
@@ -1978,17 +1979,21 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                 waves_use = hit->second.first;
                 mblk_use = hit->second.second;
             } else {
+                // the schedule (CTAs per SM) and the tile shape (m-block width: the MMA's N)
                 const double cand[] = {1.0, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0};
+                const int mcand[] = {MBLK, 64};
                 const int ls[3] = {std::max(1, lmax_g / 4), std::max(1, lmax_g / 2), std::max(1, (3 * lmax_g) / 4)};
                 cudaEvent_t e0, e1;
                 CG_CUDA_TRY(cudaEventCreate(&e0));
                 CG_CUDA_TRY(cudaEventCreate(&e1));
                 double best = 1e300;
                 waves_use = 1.0;
+                mblk_use = MBLK;
                 Sched S;
                 for (int rep = 0; rep < 2; ++rep)
+                    for (int mc : mcand)
                     for (double w : cand) {
-                        schedule(w, MBLK, S);
+                        schedule(w, mc, S);
                         s = upload(S);
                         if (s != CATANA_OK) return s;
                         CG_CUDA_TRY(cudaEventRecord(e0, st));
@@ -2007,6 +2012,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
                         if (rep == 1 && ms < best) {
                             best = ms;
                             waves_use = w;
+                            mblk_use = mc;
                         }
                     }
                 cudaEventDestroy(e0);
