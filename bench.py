@@ -767,7 +767,7 @@ def main():
         kernel = "k_fp64_raw_l"
     achieved = (kfl.value / (kms.value / 1e3)) / 1e12 if kms.value > 0 else None
     # DRAM bytes of an average k_split_l launch: the ncu capture of l = 200 on 300k points
-    # (profiles/k_split_l_l200_300k_full.md) read+wrote 756.5 MB = 1.025 x the algorithmic
+    # (profiles/k_split_l_l200_300k_full.md) read+wrote 756.0 MB = 1.024 x the algorithmic
     # 12 B per (point, m) of Legendre rows + 48 B per point (738 MB); the traffic grows in
     # proportion to points x (l + 1), so that ratio is applied here to this run's catalog
     # pieces and averaged over the launches.
@@ -775,7 +775,7 @@ def main():
     if a.form == "split":
         chunk = min(a.points, int(16e9 / (12.0 * L)))
         avg = sum((12.0 * (l + 1) + 48.0) * chunk for l in range(L)) / L
-        traffic = 1.025 * avg
+        traffic = 1.024 * avg
     if a.form == "split":
         peak_note = peak_note.replace("0.0 s step", "%.1f s step" % (ms_step / 1e3))
     roof = {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
