@@ -58,6 +58,9 @@ def parse():
                    help="skip the full-catalog FP64 comparison (about four minutes of FP64 GPU work)")
     p.add_argument("--stream-chunks", type=int, default=2,
                    help="8M-point chunks of the streamed lmax 512 / nmax 256 survey leg (0 skips it)")
+    p.add_argument("--stream-points", type=int, default=8_000_000,
+                   help="points per chunk of the streamed survey leg (the survey's chunks hold 8M; smaller "
+                        "chunks make a case small enough for a kernel profile)")
     p.add_argument("--only", default=None, choices=["side", "batched", "streamed", "next"],
                    help="time one secondary workload alone (side: FP64 100k and HEALPix nside 256) and print "
                         "its JSON")
@@ -678,7 +681,8 @@ def main():
         sp0 = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         run_one = {"side": lambda: side_workloads(torch, _lib, catana, sp0),
                    "batched": lambda: batched_workload(torch, _lib, catana, sp0),
-                   "streamed": lambda: streamed_workload(torch, _lib, catana, chunks=max(1, a.stream_chunks)),
+                   "streamed": lambda: streamed_workload(torch, _lib, catana, chunks=max(1, a.stream_chunks),
+                                                         chunk=a.stream_points),
                    "next": lambda: next_rows_workload(torch, _lib, catana)}[a.only]
         print(json.dumps({"only": a.only, "result": run_one()}, default=float))
         return
@@ -842,7 +846,8 @@ def main():
             out["side"]["next_rows"] = next_rows_workload(torch, _lib, catana)
             if a.stream_chunks > 0:
                 out["side"]["streamed_survey_l512_n256_split"] = streamed_workload(torch, _lib, catana,
-                                                                                  chunks=a.stream_chunks)
+                                                                                  chunks=a.stream_chunks,
+                                                                                  chunk=a.stream_points)
         # ---- CPU baseline: the oracle's OpenMP restatement, fixed + per-point fit ----
         t_full, _, _, note = cpu_fit(a)
         v = a.points * nmodes / t_full
