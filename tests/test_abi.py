@@ -110,6 +110,11 @@ def test_sfb_argument_validation():
         catana.sfb_decomposition(np.ones((3, 3)), 4, 4, 10.0)
     with pytest.raises(ValueError):
         catana.sfb_decomposition(pc, 4, 4, 10.0, precision="half")
+    # batched: one value per catalog where lists are given; work items of 128 or 64 complex m
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc, pc], [4, 4, 4], 4, 10.0, verbose=False)
+    with pytest.raises(ValueError):
+        catana.sfb_decomposition_batched([pc], 4, 4, 10.0, verbose=False, mblock=32)
 
 
 def test_poly_jl_rejected_where_unsupported():
