@@ -209,9 +209,9 @@ def side_workloads(torch, _lib, catana, sp, fp64_peak=None):
     d_c = torch.zeros_like(d_k)
     d_f = torch.zeros(2 * fc, dtype=torch.float64, device="cuda")
 
-    def run():
+    def run(jl=_lib.JL_AUTO):
         _lib.check(_lib.lib.catana_gpu_sfb_raw_dev(ctypes.c_void_p(d_pts.data_ptr()), None, 100000, L, M, 1000.0,
-                                                   _lib.FORM_PLAIN, ctypes.c_void_p(d_k.data_ptr()),
+                                                   _lib.FORM_PLAIN | jl, ctypes.c_void_p(d_k.data_ptr()),
                                                    ctypes.c_void_p(d_c.data_ptr()), ctypes.c_void_p(d_f.data_ptr()),
                                                    None, sp), "fp64")
     for _ in range(3):
@@ -235,6 +235,17 @@ def side_workloads(torch, _lib, catana, sp, fp64_peak=None):
                                                   "peak": pk, "unit": "TFLOP/s",
                                                   "frac": (ktf / pk) if pk else None,
                                                   "peak_source": "measured in this run (catana_gpu_fp64_peak)"}}
+    # the same case with exact j_l per (point, l, n) (the reference's branch for N <= 1000)
+    run(_lib.JL_EXACT)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(3):
+        run(_lib.JL_EXACT)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_x = e0.elapsed_time(e1) / 3
+    res["plain_fp64_100k_l32_n32"]["exact_jl"] = {"value": 100000 * modes(L, M) / (ms_x / 1e3), "unit": UNIT,
+                                                  "ms_per_step": ms_x}
     # HEALPix
     R = HP_RADIUS
     pc = catana.PointContainer(healpix_catalog(), "cartesian")

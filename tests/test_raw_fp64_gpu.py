@@ -51,12 +51,14 @@ def test_random_catalogs(cuda_device, n, lmax, nmax, interp):
     _compare(res, k, c, f)
 
 
-def test_config1_size(cuda_device):
+@pytest.mark.parametrize("interp", ["auto", "off"])
+def test_config1_size(cuda_device, interp):
     """Plain raw SFB at the reference's CPU-runnable case: 100k points uniform in a
-    ball of rmax=1000, lmax=nmax=32, seed 0 (interpolated, N > 1000)."""
+    ball of rmax=1000, lmax=nmax=32, seed 0, in the interpolated mode (the reference's
+    rule for N > 1000) and with exact j_l."""
     pts = uniform_ball(100000, 1000.0, seed=0)
-    res = catana.sfb_decomposition(catana.PointContainer(pts), 32, 32, 1000.0, True, False)
-    k, c, f = O.sfb_raw(pts, 32, 32, 1000.0, interpolated=True)
+    res = catana.sfb_decomposition(catana.PointContainer(pts), 32, 32, 1000.0, True, False, interpolation=interp)
+    k, c, f = O.sfb_raw(pts, 32, 32, 1000.0, interpolated=(interp == "auto"))
     _compare(res, k, c, f)
 
 
