@@ -142,7 +142,7 @@ struct SplitCatInput {
     double kmax = 0.0;            // > 0: keep only k_ln <= kmax
     double *kln_dev = nullptr;    // k_ln (lmax x nmax), already on the device
     double *f_acc = nullptr;      // packed complex f_lmn accumulator
-    bool accurate = false;        // CATANA_SPLIT_ACCURATE: Reinsch-modified Legendre rows
+    bool accurate = false;        // CATANA_SPLIT_ACCURATE: Reinsch-modified Legendre rows (always above lmax 256)
 };
 // Split form over several catalogs: level-synchronous launches over all of them,
 // optionally captured as one CUDA graph.  `waves` = CTAs per SM each level's work

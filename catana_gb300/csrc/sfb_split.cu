@@ -101,10 +101,9 @@ constexpr uint32_t SM_STROW = MBLK * KT * 4;           // one row set (MBLK m x 
 constexpr uint32_t SM_STPTS = KT * 48;                 // the tile's 32 SplitPt records
 constexpr uint32_t SM_STEXP = MBLK * 8;                // row exponent words of one row set (extended range)
 // one stage: P_{l-1}, P_{l-2} (Reinsch-modified rows: X_{l-1}), the points and, extended
-// range, the exponent words of both row sets (Reinsch-modified rows: one word serves
-// P_{l-1} and X_{l-1})
+// range, the exponent words (one word serves P_{l-1} and X_{l-1})
 __host__ __device__ constexpr uint32_t sm_stage(bool ext, bool rs) {
-    return 2 * SM_STROW + SM_STPTS + (ext ? (rs ? 1u : 2u) * SM_STEXP : 0u);
+    return 2 * SM_STROW + SM_STPTS + (ext ? SM_STEXP : 0u);
 }
 // after the stages: per n pair (kz_hi, kz_lo) x 2; J scale 2^s_ln per n; readout 2^-s_ln 2^-12 per
 // n; recurrence coefficients of the m pairs (and of the Reinsch-modified step); per operand warp
@@ -117,9 +116,7 @@ __host__ __device__ constexpr uint32_t off_js(bool ext, bool rs, int nst) { retu
 __host__ __device__ constexpr uint32_t off_inv(bool ext, bool rs, int nst) { return off_js(ext, rs, nst) + NHALF * 4; }
 __host__ __device__ constexpr uint32_t off_coef(bool ext, bool rs, int nst) { return off_inv(ext, rs, nst) + NHALF * 4; }
 __host__ __device__ constexpr uint32_t off_rcoef(bool ext, bool rs, int nst) { return off_coef(ext, rs, nst) + MBLK * 16; }
-__host__ __device__ constexpr uint32_t off_jt(bool ext, bool rs, int nst) {
-    return off_rcoef(ext, rs, nst) + (ext && !rs ? 0u : MBLK * 16);
-}
+__host__ __device__ constexpr uint32_t off_jt(bool ext, bool rs, int nst) { return off_rcoef(ext, rs, nst) + MBLK * 16; }
 __host__ __device__ constexpr uint32_t off_tab(bool ext, bool rs, int nst) {
     return off_jt(ext, rs, nst) + (uint32_t)NOPW * JPW * 8 * 4;
 }
@@ -128,7 +125,6 @@ constexpr uint32_t smem_bytes(bool ext, bool rs, int nst, int nint) {
     return off_tab(ext, rs, nst) + (uint32_t)nint * 32 + 1024;
 }
 constexpr uint32_t SMEM_LIMIT = 232448 - 1024;  // per block, leaving room for the static part
-static_assert(smem_bytes(true, false, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
 static_assert(smem_bytes(true, true, 2, NINT_MAX) <= SMEM_LIMIT, "k_split_l shared memory");
 // J of a tile comes from a cubic Taylor expansion about its record-16 radius when
 // k_max max|r - r_c| <= JT_TAU: the omitted terms are below JT_TAU^4 / 24 ~ 7e-9 of j_l's
@@ -165,10 +161,10 @@ struct SplitCat {
     int lrp;                // lrows rounded up to even (m pairs per tile block: lrp / 2)
     int kzw;                // row width of kz (the catalog's nmax)
     int epitch;             // exponent words per tile (lrows rounded up to even)
-    unsigned long long *rexp;  // extended range: exponent sets [tile][lrows], set k at rexp + k * eset (three-term
-                               // rows: three rotating with l % 3; Reinsch-modified rows: 0, 1 by the parity of l)
+    unsigned long long *rexp;  // extended range: exponent sets [tile][lrows] by the parity of l, set k at
+                               // rexp + k * eset (one word per value serves P_l and X_l)
     int64_t eset;           // words per exponent set
-    const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..3, exponent words of sets 0..2 at 4..6
+    const char *tmaps;      // TMA descriptors (128 B each): rows of sets 0..3, exponent words of sets 0, 1 at 4, 5
     const float4 *kz;       // [l][kzw]: (k_ln / H as float-float, J scale 2^s_ln, 1 / (2^s_ln 2^12))
     const int *nmax_l;      // [l]: radial orders computed at l (kmax cut)
 };
@@ -232,10 +228,11 @@ __device__ __forceinline__ void phase_seed(unsigned long long u, int m, float &c
 
 // One CTA: multipole l, complex m in [128 b, 128 b + 128) of it (blockIdx.y = b),
 // a slab of 32-point tiles (blockIdx.x).
-// EXT: rows carry a 2-bit exponent per (point, m) -- the stored value is
-// P * 2^100 * 2^(128 e); e grows by one when a sectoral value drops below 2^-40 and
-// shrinks by one when a value grows past 2^40 along l, so seeds down to ~2^-520 stay
-// exact.  Values with e > 0 are below 2^-188 and enter Y as zero.
+// EXT (lmax > 256, always with the Reinsch-modified rows, RS): rows carry a 2-bit
+// exponent per (point, m) -- the stored value is P * 2^100 * 2^(128 e); e grows by one
+// when a sectoral value drops below 2^-40 and shrinks by one when a value grows past 2^40
+// along l, so seeds down to ~2^-520 stay exact.  P_l and D_l of a level share the
+// exponent.  Values with e > 0 are below 2^-188 and enter Y as zero.
 // FULLJ: every item of the launch has 128 radial orders in its half (no kmax cut):
 // with 16 operand warps each evaluates 8 J rows; otherwise the items' live row pairs
 // are spread over the warps and the rest of J stays zero.
@@ -308,6 +305,7 @@ __device__ __forceinline__ float2 sum_once2(float2 rh, float2 rl, float2 p, floa
 
 template <bool EXT, bool FULLJ, int NST, bool RS>
 __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
+    static_assert(!EXT || RS, "the extended range takes the Reinsch-modified rows");
     constexpr uint32_t STG = sm_stage(EXT, RS);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -403,10 +401,10 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // the rows this level writes: P_l (and, Reinsch-modified rows, X_l)
     float *__restrict__ st0 = cat.rows + (size_t)(RS ? (l & 1) : l % 3) * set;
     float *__restrict__ xt0 = cat.rows + (size_t)(RS ? 2 + (l & 1) : 0) * set;
-    // extended range: the exponent words this level writes (three-term rows: sets rotating
-    // with l % 3 like the rows; Reinsch-modified rows: by the parity of l, one word for P_l and X_l)
+    // extended range: the exponent words this level writes (set by the parity of l, one word
+    // for P_l and X_l)
     unsigned long long *ex0 = nullptr;
-    if (EXT) ex0 = cat.rexp + (size_t)(RS ? (l & 1) : l % 3) * cat.eset;
+    if (EXT) ex0 = cat.rexp + (size_t)(l & 1) * cat.eset;
     float *__restrict__ partial_cta = a.partial + (size_t)blockIdx.x * 256 * 128;
 
     uint32_t uses0 = 0, uses1 = 0, waited0 = 0, waited1 = 0;  // commits / completed waits per buffer
@@ -430,24 +428,20 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
     // records (one bulk copy), the rows P_{l-1}(m) and P_{l-2}(m) of this block's m in
     // 32-row TMA boxes (rows past the tensor's end arrive as zeros; slots the step does
     // not read -- the sectoral m = l of P_{l-1}, m > l-2 of P_{l-2} -- hold stale rows),
-    // and (extended range) the exponent words of both sets (Reinsch-modified rows: of level l-1)
+    // and (extended range) the exponent words of level l-1
     // staged rows: P_{l-1} and P_{l-2} (three-term rows) or X_{l-1} (Reinsch-modified rows);
-    // descriptors 0..3 are the row sets, 4..6 the exponent sets
+    // descriptors 0..3 are the row sets, 4 and 5 the exponent sets
     const char *tm_r1 = cat.tmaps + 128 * (RS ? (l + 1) & 1 : (l + 2) % 3);
     const char *tm_r2 = cat.tmaps + 128 * (RS ? 2 + ((l + 1) & 1) : (l + 1) % 3);
-    const char *tm_e1 = cat.tmaps + 128 * (4 + (RS ? (l + 1) & 1 : (l + 2) % 3));
-    const char *tm_e2 = cat.tmaps + 128 * (4 + (l + 1) % 3);
+    const char *tm_e1 = cat.tmaps + 128 * (4 + ((l + 1) & 1));
     const int nb1 = l > 0 ? (mcount + 31) >> 5 : 0;
     const int nb2 = (max(0, min(mcount, RS ? l - mb0 : l - 1 - mb0)) + 31) >> 5;
     const uint32_t stage_bytes =
-        SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? (RS ? 1u : 2u) * SM_STEXP : 0u);
+        SM_STPTS + 4096u * (uint32_t)(nb1 + nb2) + ((EXT && l > 0) ? SM_STEXP : 0u);
     if (tid == 0) {  // descriptors rewritten by the host between launches: read them afresh
         tc05::tmap_acquire(tm_r1);
         tc05::tmap_acquire(tm_r2);
-        if (EXT) {
-            tc05::tmap_acquire(tm_e1);
-            if (!RS) tc05::tmap_acquire(tm_e2);
-        }
+        if (EXT) tc05::tmap_acquire(tm_e1);
     }
     auto prefetch = [&](int64_t j) {
         const int64_t t = t0 + j;
@@ -463,10 +457,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
         for (int k = 0; k < nb1; ++k) tc05::tma_load_2d(stg + k * 4096, tm_r1, (int)(2 * KT * t), (mb0 >> 1) + 16 * k, &sbar[sidx]);
         for (int k = 0; k < nb2; ++k)
             tc05::tma_load_2d(stg + SM_STROW + k * 4096, tm_r2, (int)(2 * KT * t), (mb0 >> 1) + 16 * k, &sbar[sidx]);
-        if (EXT && l > 0) {
-            tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
-            if (!RS) tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS + SM_STEXP, tm_e2, mb0, (int)t, &sbar[sidx]);
-        }
+        if (EXT && l > 0) tc05::tma_load_2d(stg + 2 * SM_STROW + SM_STPTS, tm_e1, mb0, (int)t, &sbar[sidx]);
     };
     // the load of tile t0 + j is the (j / NST)-th completion of its stage's barrier
     auto wait_stage = [&](int64_t j, uint64_t limit) -> bool {
@@ -574,7 +565,6 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
             const float *stg2 = stg1 + MBLK * KT;
             const unsigned long long *stge1 = reinterpret_cast<const unsigned long long *>(
                 sm + OFF_ST + (uint32_t)sidx * STG + 2 * SM_STROW + SM_STPTS);
-            const unsigned long long *stge2 = stge1 + MBLK;
             // this thread's point record in three 16-byte loads (at the records' 48-byte stride
             // these are free of bank conflicts, the fields one by one are not)
             const uint4 *prec = reinterpret_cast<const uint4 *>(sm + OFF_ST + (uint32_t)sidx * STG +
@@ -942,16 +932,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                 // both m take the plain three-term step: packed arithmetic
                                 const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
                                 const float2 p1 = reinterpret_cast<const float2 *>(stg1)[(ml >> 1) * KT + q];
-                                float2 p2 = reinterpret_cast<const float2 *>(stg2)[(ml >> 1) * KT + q];
-                                unsigned ea = 0, eb = 0;  // extended range: exponents of P_{l-1} at m, m+1
-                                if (EXT) {
-                                    ea = ebits(stge1[ml], q);
-                                    eb = ebits(stge1[ml + 1], q);
-                                    const unsigned fa = ebits(stge2[ml], q), fb = ebits(stge2[ml + 1], q);
-                                    // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                    if (fa != ea) p2.x = (fa == ea + 1) ? p2.x * 0x1p-64f * 0x1p-64f : 0.f;
-                                    if (fb != eb) p2.y = (fb == eb + 1) ? p2.y * 0x1p-64f * 0x1p-64f : 0.f;
-                                }
+                                const float2 p2 = reinterpret_cast<const float2 *>(stg2)[(ml >> 1) * KT + q];
                                 const float2 tt = __ffma2_rn(xh2, p1, __fmul2_rn(xl2, p1));
                                 if (m == 0) {  // the m = 0 column rounded once (step_once)
                                     P = step_once2(make_float2(ca.x, ca.y), make_float2(ca.z, ca.w),
@@ -963,31 +944,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                         __ffma2_rn(make_float2(ca.z, ca.w), tt, make_float2(-bb.x, -bb.y));
                                     P = __ffma2_rn(make_float2(ca.x, ca.y), tt, vv);
                                 }
-                                if (EXT) {  // renormalise values that grew past 2^40 while e > 0
-                                    if (ea > 0 && fabsf(P.x) > 0x1p40f) {
-                                        P.x = P.x * 0x1p-64f * 0x1p-64f;
-                                        --ea;
-                                    }
-                                    if (eb > 0 && fabsf(P.y) > 0x1p40f) {
-                                        P.y = P.y * 0x1p-64f * 0x1p-64f;
-                                        --eb;
-                                    }
-                                }
                                 if (wrows) *reinterpret_cast<float2 *>(rowp) = P;
-                                if (EXT && wrows) {
-                                    const unsigned a0 = __ballot_sync(0xffffffffu, ea & 1u);
-                                    const unsigned a1 = __ballot_sync(0xffffffffu, (ea >> 1) & 1u);
-                                    const unsigned b0 = __ballot_sync(0xffffffffu, eb & 1u);
-                                    const unsigned b1 = __ballot_sync(0xffffffffu, (eb >> 1) & 1u);
-                                    if (lane == 0) {
-                                        ex0[t * cat.epitch + m] = ((unsigned long long)a1 << 32) | a0;
-                                        ex0[t * cat.epitch + m + 1] = ((unsigned long long)b1 << 32) | b0;
-                                    }
-                                }
-                                if (EXT) {  // values with e > 0 are below 2^-188: no contribution
-                                    if (ea) P.x = 0.f;
-                                    if (eb) P.y = 0.f;
-                                }
                             } else {
                                 // sectoral (m = l), m = l - 1, or the block's last odd m
                                 const float4 ca = s_coef[ml], cb = s_coef[ml + 1];
@@ -996,54 +953,31 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
                                 for (int h = 0; h < 2; ++h) {
                                     const int mlh = ml + h, mh = m + h;
                                     float Pq = 0.f;
-                                    unsigned e = 0;
                                     if (mlh < mhi) {  // warp-uniform
                                         if (l == 0) {
                                             Pq = P00_SCALED;
                                         } else if (mh == l) {
                                             // the FP64 sectoral seed, rounded once by k_split_sectoral
-                                            // into slot l of the P_{l-1} set (EXT: with its exponent)
+                                            // into slot l of the P_{l-1} set
                                             Pq = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
-                                            if (EXT) e = ebits(stge1[mlh], q);
                                         } else if (mh == l - 1) {
                                             // P_{l,l-1} = sqrt(2l+1) x P_{l-1,l-1}, rounded once
                                             const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
                                             const float p1 = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
-                                            if (EXT) e = ebits(stge1[mlh], q);
                                             const float tt = fmaf(xh, p1, xl * p1);
                                             Pq = step_once(A_hi, A_lo, 0.f, 0.f, tt, 0.f);
-                                            if (EXT && e > 0 && fabsf(Pq) > 0x1p40f) {
-                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
-                                                --e;
-                                            }
                                         } else {  // m <= l - 2: one recurrence step, rounded once
                                             const float A_hi = h ? ca.y : ca.x, A_lo = h ? ca.w : ca.z;
                                             const float B_hi = h ? cb.y : cb.x, B_lo = h ? cb.w : cb.z;
                                             const float p1 = stg1[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
-                                            float p2 = stg2[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
-                                            if (EXT) {  // exponents of P_{l-1} and P_{l-2}
-                                                e = ebits(stge1[mlh], q);
-                                                const unsigned e2 = ebits(stge2[mlh], q);
-                                                // along l the exponent only shrinks: align P_{l-2} to P_{l-1}
-                                                if (e2 != e) p2 = (e2 == e + 1) ? p2 * 0x1p-64f * 0x1p-64f : 0.f;
-                                            }
+                                            const float p2 = stg2[((mlh >> 1) * KT + q) * 2 + (mlh & 1)];
                                             const float tt = fmaf(xh, p1, xl * p1);
                                             // rounded once (step_once); at l = 2, m = 0 P_{l-2} = P_00
                                             // is the same for every point, so the fma chain's error
                                             // would even be one constant shared by all points
                                             Pq = step_once(A_hi, A_lo, B_hi, B_lo, tt, p2);
-                                            if (EXT && e > 0 && fabsf(Pq) > 0x1p40f) {
-                                                Pq = Pq * 0x1p-64f * 0x1p-64f;
-                                                --e;
-                                            }
                                         }
                                         if (wrows) rowp[h] = Pq;
-                                        if (EXT && wrows) {
-                                            const unsigned b0w = __ballot_sync(0xffffffffu, e & 1u);
-                                            const unsigned b1w = __ballot_sync(0xffffffffu, (e >> 1) & 1u);
-                                            if (lane == 0) ex0[t * cat.epitch + mh] = ((unsigned long long)b1w << 32) | b0w;
-                                        }
-                                        if (EXT && e != 0) Pq = 0.f;  // below 2^-188: no contribution
                                     }
                                     pv[h] = Pq;
                                 }
@@ -1160,7 +1094,7 @@ __global__ void __launch_bounds__(NTOT, 1) k_split_l(SplitArgs a) {
 // frame of the running 2-bit exponent (stored value P 2^100 2^(128 e), e raised when
 // the value drops below 2^-40, 0 below 2^-520), with the exponent word written too.
 // mode bit 0: Reinsch-modified rows (sets by the parity of l, records carrying 1 - |cos(theta)|);
-// bit 1: extended range (exponent words, sets of the three-term rows rotating with l % 3)
+// bit 1: extended range (exponent words; always with bit 0)
 __global__ void k_split_sectoral(const SplitCat *cats, int cat, int lmax, const double *__restrict__ asect,
                                  int64_t ntiles, int mode) {
     const bool rs = (mode & 1) != 0, ext = (mode & 2) != 0;
@@ -1590,8 +1524,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         void (*const kerns[])(SplitArgs) = {
             k_split_l<false, true, 2, false>, k_split_l<false, false, 2, false>, k_split_l<false, true, 3, false>,
             k_split_l<false, false, 3, false>, k_split_l<false, true, 2, true>,  k_split_l<false, false, 2, true>,
-            k_split_l<false, true, 3, true>,  k_split_l<false, false, 3, true>,  k_split_l<true, true, 2, false>,
-            k_split_l<true, false, 2, false>, k_split_l<true, true, 2, true>,   k_split_l<true, false, 2, true>};
+            k_split_l<false, true, 3, true>,  k_split_l<false, false, 3, true>,  k_split_l<true, true, 2, true>,
+            k_split_l<true, false, 2, true>};
         for (auto kf : kerns)
             CG_CUDA_TRY(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LIMIT));
         ctx->attr_split = true;
@@ -1685,7 +1619,9 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         const bool ext = lmax_g > SPLIT_LMAX;  // extended-range rows (2-bit exponents)
         // row sets: Reinsch-modified rows P_l, X_l by the parity of l (X = D or P_{l-1});
         // three-term rows P_l, P_{l-1}, P_{l-2} rotating
-        const bool rs = accurate;  // Reinsch-modified rows (CATANA_SPLIT_ACCURATE)
+        // Reinsch-modified rows: with CATANA_SPLIT_ACCURATE, and always in the extended range
+        // (there the three-term rows lose a few 1e-6 for points near a pole)
+        const bool rs = accurate || ext;
         const int nsets = rs ? 4 : 3;
         // three stages (tiles staged two ahead) where shared memory allows: plain rows and a
         // table of at most ~750 intervals; otherwise two
@@ -1694,10 +1630,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         // kernel per level: extended-range rows above lmax 256; the full-J layout when every
         // item of the level has 128 radial orders in its half
         auto kern_for = [&](bool full) {
-            if (ext) {
-                if (rs) return full ? k_split_l<true, true, 2, true> : k_split_l<true, false, 2, true>;
-                return full ? k_split_l<true, true, 2, false> : k_split_l<true, false, 2, false>;
-            }
+            if (ext) return full ? k_split_l<true, true, 2, true> : k_split_l<true, false, 2, true>;
             if (rs) {
                 if (nst == 3) return full ? k_split_l<false, true, 3, true> : k_split_l<false, false, 3, true>;
                 return full ? k_split_l<false, true, 2, true> : k_split_l<false, false, 2, true>;
@@ -1718,7 +1651,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             off_rows[c - c0] = ws_bytes;
             ws_bytes += al256((size_t)nsets * cats[c].stride * ((cats[c].in.lmax + 1) & ~1) * sizeof(float));
             off_exp[c - c0] = ws_bytes;
-            if (ext) ws_bytes += al256((size_t)3 * exp_set_words(cats[c]) * sizeof(unsigned long long));
+            if (ext) ws_bytes += al256((size_t)2 * exp_set_words(cats[c]) * sizeof(unsigned long long));
         }
         CG_CUDA_TRY(ctx->split_ws.ensure(ws_bytes));
         char *ws = ctx->split_ws.as<char>();
@@ -1760,8 +1693,8 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
         std::vector<size_t> o_kz(gn), o_nl(gn), o_tm(gn);
         for (int c = c0; c < c1; ++c) {
             // TMA descriptors 0..3: the Legendre row sets (m pairs interleaved per point:
-            // [lrp / 2][2 stride] FP32, 64 x 16 boxes = 32 m x 32 points); 4..6, extended
-            // range: the exponent sets ([tile][epitch] words, 128 x 1 boxes)
+            // [lrp / 2][2 stride] FP32, 64 x 16 boxes = 32 m x 32 points); 4, 5, extended
+            // range: the exponent sets by the parity of l ([tile][epitch] words, 128 x 1 boxes)
             CatPlan &P = cats[c];
             CUtensorMap tm[8];
             memset(tm, 0, sizeof(tm));
@@ -1777,7 +1710,7 @@ catana_status_t split_run(DeviceContext *ctx, std::vector<SplitCatInput> &cats_i
             if (ext) {
                 const int ep = (P.in.lmax + 1) & ~1;
                 char *ex = ws + off_exp[c - c0];
-                for (int k = 0; k < 3; ++k)
+                for (int k = 0; k < 2; ++k)
                     if (!tmap_2d(&tm[4 + k], CU_TENSOR_MAP_DATA_TYPE_UINT64, ex + (size_t)k * exp_set_words(P) * 8,
                                  (uint64_t)ep, (uint64_t)P.ntiles, (uint64_t)ep * 8, 128, 1)) {
                         set_error("cuTensorMapEncodeTiled failed for the row exponents");

@@ -13,7 +13,8 @@ Keyword extensions (absent in the reference, defaults reproduce it):
                        'split': tcgen05 tensor cores, 3-term FP16 hi+lo products;
                        'split_accurate': the same with Reinsch-modified Legendre
                        rows: half the f_lmn error at high l (ten times less near
-                       the poles), ~12% slower
+                       the poles), ~12% slower; above lmax 256 'split' always
+                       takes these rows
   interpolation='auto' 'auto' (interpolated iff N > 1000, the reference's rule),
                        'on' (linear table), 'off' (exact j_l) or 'poly' (piecewise
                        FP64 polynomials, as accurate as 'off' at the cost of 'on';

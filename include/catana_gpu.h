@@ -69,12 +69,13 @@ typedef enum {
 #define CATANA_FORM_SPLIT 4u
 #define CATANA_FORM_MASK 4u
 /* Split form (no counterpart in the reference): the Legendre rows follow the
- * Reinsch-modified recurrence at |cos(theta)| for m < 128 -- rows P_l and
+ * Reinsch-modified recurrence at |cos(theta)| for m < 128 (above lmax 256 always, with
+ * or without this flag) -- rows P_l and
  * D_l = P_l - rho_l P_{l-1}, rho_l the ratio of consecutive P_lm / sin^m(theta) at the
  * pole -- so FP32 rounding no longer accumulates through the three-term recurrence's
  * cancellation near the poles.  About half the f_lmn error at high l of the default
  * split form, and up to ten times less for points near a pole, at ~12% lower
- * throughput (one more row written per value).  Ignored by the plain form. */
+ * throughput at lmax 256 (one more row written per value).  Ignored by the plain form. */
 #define CATANA_SPLIT_ACCURATE 32u
 /* HEALPix path: 0 reproduces the reference's m-extraction, which reads
  * F[rpix - m%rpix] without conjugation when m%rpix > rpix/2
