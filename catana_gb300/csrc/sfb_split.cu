@@ -32,9 +32,9 @@
 //     representable (enough for lmax <= 256; above, each value carries a 2-bit exponent);
 //     the m = 0 step is rounded once (step_once), so Y_l0 carries no mean error over the
 //     sphere through which a catalog's monopole could leak into l > 0.  With
-//     CATANA_SPLIT_ACCURATE the columns m < 128 follow the Reinsch-modified recurrence
-//     at |cos(theta)| instead (rows P_l and D_l = P_l - rho_l P_{l-1}), whose rounding
-//     does not build up near the poles;
+//     CATANA_SPLIT_ACCURATE, and always above lmax 256, the columns m < 128 follow the
+//     Reinsch-modified recurrence at |cos(theta)| instead (rows P_l and
+//     D_l = P_l - rho_l P_{l-1}), whose rounding does not build up near the poles;
 //   * the sectoral seeds stay FP64: before the level loop, k_split_sectoral advances
 //     every point's P_ll = -sqrt((2l+1)/(2l)) s P_{l-1,l-1} in FP64 from the FP32
 //     value of P_00 and stores each level's P_ll, rounded once, in slot m = l of the
